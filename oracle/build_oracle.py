@@ -1,0 +1,139 @@
+"""Build recipe for the test oracle (test infrastructure only).
+
+* ``oracle/liboracle.so`` -- the FP64 CPU restatement in ``mpm_oracle.c``
+  (gcc + OpenMP).  Built on every machine that runs the tests.
+* ``oracle/_ref/libref32.so`` / ``libref64.so`` -- the reference's own
+  DiffMPMLib3D sources compiled together with ``ref_driver.cpp``.  Built only
+  where the reference tree is present (``REF_DIR``, default the read-only
+  mount).  The sources are read where they lie; the FP64 variant and the
+  ``private:`` -> ``public:`` edit (so the driver can set CompGraph's dt, drag
+  and smoothing) are applied to temporary copies outside this repository.
+  Only the two shared libraries are written into ``oracle/_ref/``.
+
+Usage: ``python oracle/build_oracle.py [--no-ref] [--force]``
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT_REF = HERE / "_ref"
+REF_DIR = Path(os.environ.get("REF_DIR", "/root/reference"))
+
+REF_SOURCES = [
+    "ForwardSimulation.cpp", "BackPropagation.cpp", "Elasticity.cpp", "PointCloud.cpp",
+    "Grid.cpp", "GridNode.cpp", "MaterialPoint.cpp", "CompGraph.cpp", "Tensor3x3x3x3.cpp",
+]
+CXXFLAGS = ["-std=c++17", "-O2", "-fopenmp", "-fPIC", "-fno-fast-math", "-ffp-contract=off",
+            "-DNDEBUG", "-DEIGEN_NO_DEBUG", "-D_USE_MATH_DEFINES", "-w"]
+
+
+def _newer(out: Path, inputs) -> bool:
+    if not out.exists():
+        return False
+    t = out.stat().st_mtime
+    return all(Path(i).stat().st_mtime <= t for i in inputs)
+
+
+def build_oracle(force: bool = False) -> Path:
+    src = HERE / "mpm_oracle.c"
+    out = HERE / "liboracle.so"
+    if force or not _newer(out, [src]):
+        cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c99", "-ffp-contract=off",
+               str(src), "-o", str(out), "-lm"]
+        subprocess.check_call(cmd)
+    return out
+
+
+_FLOAT_LIT = re.compile(r"\b((?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?)f\b")
+
+
+def _widen(text: str) -> str:
+    """float -> double, Eigen *f types -> *d, strip float literal suffixes."""
+    text = re.sub(r"\bVector3f\b", "Vector3d", text)
+    text = re.sub(r"\bMatrix3f\b", "Matrix3d", text)
+    text = re.sub(r"\bMatrixXf\b", "MatrixXd", text)
+    text = re.sub(r"\bVectorXf\b", "VectorXd", text)
+    text = re.sub(r"\bfloat\b", "double", text)
+    return _FLOAT_LIT.sub(r"\1", text)
+
+
+def _stage(tmp: Path, widen: bool) -> Path:
+    """Copy DiffMPMLib3D into tmp with the mechanical edits applied."""
+    dst = tmp / ("src64" if widen else "src32")
+    dst.mkdir(parents=True, exist_ok=True)
+    for f in (REF_DIR / "DiffMPMLib3D").iterdir():
+        if f.suffix not in (".h", ".cpp"):
+            continue
+        text = f.read_text(encoding="utf-8", errors="replace")
+        if f.name == "CompGraph.h":
+            text = text.replace("private:", "public:")
+        if widen:
+            text = _widen(text)
+        (dst / f.name).write_text(text, encoding="utf-8")
+    return dst
+
+
+def _compile(args):
+    cmd, = args
+    subprocess.check_call(cmd)
+
+
+def build_ref(force: bool = False) -> list[Path]:
+    if not (REF_DIR / "DiffMPMLib3D" / "ForwardSimulation.cpp").exists():
+        return []
+    OUT_REF.mkdir(exist_ok=True)
+    outs = []
+    inputs = [HERE / "ref_driver.cpp", Path(__file__)] + [REF_DIR / "DiffMPMLib3D" / s for s in REF_SOURCES]
+    todo = []
+    for widen, name in ((False, "libref32.so"), (True, "libref64.so")):
+        out = OUT_REF / name
+        outs.append(out)
+        if force or not _newer(out, inputs):
+            todo.append((widen, out))
+    if not todo:
+        return outs
+    tmp = Path(tempfile.mkdtemp(prefix="mpm_ref_"))
+    try:
+        jobs, links = [], []
+        for widen, out in todo:
+            src = _stage(tmp, widen)
+            inc = ["-I", str(src), "-I", str(REF_DIR / "include"), "-I", str(REF_DIR / "include" / "qrsvd")]
+            objs = []
+            for s in REF_SOURCES + ["ref_driver.cpp"]:
+                cpp = (HERE / s) if s == "ref_driver.cpp" else (src / s)
+                obj = tmp / f"{'64' if widen else '32'}_{s}.o"
+                objs.append(obj)
+                jobs.append(["g++", *CXXFLAGS, *inc, "-c", str(cpp), "-o", str(obj)])
+            links.append(["g++", "-shared", "-fopenmp", *map(str, objs), "-o", str(out)])
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            list(ex.map(_compile, [(j,) for j in jobs]))
+        for cmd in links:
+            subprocess.check_call(cmd)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return outs
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--no-ref", action="store_true")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args()
+    print(build_oracle(a.force))
+    if not a.no_ref:
+        for p in build_ref(a.force):
+            print(p)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
