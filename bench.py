@@ -1,0 +1,457 @@
+#!/usr/bin/env python
+"""bench.py -- fwd+bwd particle-steps/s of the differentiable MPM rollout.
+
+Workload (default ``spheres2m``): 2,000,000 particles in a union of 8 seeded
+spheres (radii 0.08-0.15) on 129^3 nodes, Fixed-Corotated material
+(E=1e4, nu=0.3, density chosen for CFL 0.45 at dt=2.5e-4), cubic B-spline
+APIC, 400 steps forward plus the exact adjoint, checkpoint every 20 steps
+with recomputation.  One bench step is one such rollout (forward 400 steps,
+loss gradient, backward 400 steps); value = particles * steps / time.
+
+`value` is timed with inputs resident in HBM; `e2e` is the same rollout
+driven through the drop-in bindings from pinned host buffers with the
+host<->device copies inside the timed region.  L2 (129 MB) is flushed with a
+256 MiB write between timed steps (outside the CUDA-event brackets).
+
+`--impl reference` times the reference algorithm's CPU path: the FP64 CPU
+restatement in oracle/ (the reference's own sources are not present on the
+GPU host), on all host threads, over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "shape-morphing-binder_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+os.environ.setdefault("MPM_QUIET", "1")
+
+METRIC = "fwd+bwd particle-steps/s on 1 GB300 vs plain FP64 GPU form at ≤1e-4 grad rel err"
+UNIT = "particle-steps/s"
+
+
+# ------------------------------------------------------------------ helpers
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(name: str, quick: bool = False):
+    from diffmpm_bindings import workloads as W
+    if name == "spheres2m":
+        w = W.spheres2m(n=200_000 if quick else 2_000_000, steps=40 if quick else 400, checkpoint=20)
+    elif name == "ellipsoid64":
+        w = W.ellipsoid64(steps=20 if quick else 100, checkpoint=10)
+    elif name == "sphere32":
+        w = W.sphere32()
+        w.checkpoint = 1
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    if w.target is None:
+        rng = np.random.default_rng(11)
+        w.target = w.x + 0.02 * np.sin(2 * np.pi * w.x[:, [1, 2, 0]] + rng.random(3))
+    return w
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- our arm
+
+# algorithmic bytes per particle and per active node for each kernel (FP32
+# storage)
+KERNEL_BYTES = {
+    "p2g": (112, 16),
+    "g2p": (148, 16),
+    "g2p_adj": (184, 16),
+    "p2g_adj": (380, 32),
+    "grid_update": (0, 32),
+    "grid_adj": (0, 48),
+}
+
+
+def build_graph(dm, w, precision, checkpoint, adjoint="exact"):
+    dt = np.float64 if precision == "fp64" else np.float32
+    pc = dm.PointCloud.from_arrays(w.x.astype(dt), v=w.v.astype(dt), F=w.F.astype(dt), m=w.m.astype(dt),
+                                   vol=w.vol.astype(dt), lam=w.lam.astype(dt), mu=w.mu.astype(dt),
+                                   precision=precision)
+    grid = dm.Grid(*w.dims, w.dx, w.grid_min, precision=precision)
+    cg = dm.CompGraph(pc, grid, grid, adjoint=adjoint, checkpoint_every=checkpoint)
+    cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
+    return cg, (pc, grid)
+
+
+def device_rollout(torch, cg, T, tgt, n):
+    """Forward T steps, position-loss gradient on device, backward T steps."""
+    cg.compute_forward_pass(0, 0)
+    last = cg.get_point_cloud(T)
+    xT = last.get_torch("x", device="cuda")
+    g = (2.0 / n) * (xT - tgt)
+    last.set("grad_x", g)
+    cg.compute_backward_pass(0)
+
+
+def run_ours(args, rank, world, device):
+    import torch
+    import diffmpm_bindings as dm
+    lib = dm._lib.lib
+    lib.mpm_set_verbose(0)
+    w = make_workload(args.workload, args.quick)
+    n, T = w.n, w.steps
+    cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
+    cg.set_up_comp_graph(T + 1)
+    stream = torch.cuda.current_stream(device)
+    cg.set_stream(stream)
+    tgt = torch.tensor(w.target, dtype=torch.float32, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    for _ in range(args.warmup):
+        device_rollout(torch, cg, T, tgt, n)
+    torch.cuda.synchronize(device)
+
+    # ---- timed region (device-resident inputs)
+    lib.mpm_profile_reset()
+    lib.mpm_profile_enable(1)
+    launches0 = lib.mpm_launch_count()
+    times = []
+    barrier(world)
+    torch.cuda.synchronize(device)
+    with Clocks(device.index if device.index is not None else 0) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            device_rollout(torch, cg, T, tgt, n)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize(device)
+    barrier(world)
+    launches = lib.mpm_launch_count() - launches0
+    lib.mpm_profile_enable(0)
+    kern = {}
+    import ctypes as C
+    for k in range(10):
+        cnt, ms = C.c_longlong(), C.c_double()
+        lib.mpm_profile_query(k, C.byref(cnt), C.byref(ms))
+        if cnt.value:
+            kern[lib.mpm_kernel_name(k).decode()] = (cnt.value, ms.value)
+    t_total = max_over_ranks(torch, sum(times), world, device)
+    value = world * n * T * args.steps / t_total
+    active = cg.active_nodes(0)
+
+    # ---- roofline of the dominant kernel
+    hbm, src = peaks()
+    top = max((k for k in kern if k in KERNEL_BYTES), key=lambda k: kern[k][1])
+    cnt, ms = kern[top]
+    bp, bn = KERNEL_BYTES[top]
+    algo = bp * n + bn * active
+    achieved = algo / (ms / cnt / 1e3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "ncu_traffic.json"
+    if tp.exists():
+        d = json.loads(tp.read_text()).get(top)
+        if d and d.get("bytes_per_particle"):
+            traffic = d["bytes_per_particle"] * n
+    total_ms = sum(v[1] for v in kern.values())
+    roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic, "algorithmic_bytes_per_launch": algo, "launches": cnt,
+            "avg_launch_ms": round(ms / cnt, 5),
+            "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][1])}}
+
+    # ---- e2e through the public API with host buffers
+    e2e = run_e2e(torch, dm, args, w, device, keep)
+
+    # ---- plain FP64 form and accuracy (rank 0)
+    fp64 = None
+    if rank == 0 and not args.no_fp64:
+        fp64 = run_fp64(torch, dm, w, device, args)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(w, args)
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * t_total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64-guarded stress)", "data": "synthetic (seeded)",
+        "config": {"workload": w.name, "particles": n, "grid_nodes": list(w.dims), "dx": w.dx, "timesteps": T,
+                   "checkpoint_every": w.checkpoint, "dt": w.dt, "density": round(w.rho, 3),
+                   "material": "fixed-corotated E=%g nu=%g" % (w.extra["E"], w.extra["nu"]),
+                   "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
+                   "l2": "flushed between timed steps (256 MiB write, outside the event brackets)",
+                   "bench_step": "one rollout: forward T steps + loss gradient + backward T steps"},
+        "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
+        "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
+    }
+    if fp64:
+        line["fp64_plain"] = fp64
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def run_e2e(torch, dm, args, w, device, keep):
+    """Public API with pinned host buffers: x0, v0, F0 in; dL/dx_T seed in
+    (computed on the host from x_T out, like run.py's gradient injection);
+    dL/dv0 and dL/dF0 out."""
+    n, T = w.n, w.steps
+    pc0, grid = keep
+    cg = dm.CompGraph(pc0, grid, grid, adjoint="exact", checkpoint_every=w.checkpoint)
+    cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
+    cg.set_up_comp_graph(T + 1)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).pin_memory()  # noqa: E731
+    hx, hv, hF = pin(w.x), pin(w.v), pin(w.F)
+    htgt = w.target.astype(np.float32)
+    out_x = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    out_gv = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    out_gF = torch.empty((n, 3, 3), dtype=torch.float32).pin_memory()
+    seed = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+    h2d = (hx.numel() + hv.numel() + hF.numel() + seed.numel()) * 4
+    d2h = (out_x.numel() + out_gv.numel() + out_gF.numel()) * 4
+    import ctypes as C
+    lib = dm._lib.lib
+
+    def get_into(pc, field, t):
+        dm._lib.check(lib.mpm_pointcloud_get(pc._h, dm._lib.FIELDS[field], C.c_void_p(t.data_ptr()), 0, 0))
+
+    def step():
+        l0 = cg.get_point_cloud(0)
+        l0.set("x", hx.numpy())
+        l0.set("v", hv.numpy())
+        l0.set("F", hF.numpy())
+        cg.compute_forward_pass(0, 0)
+        last = cg.get_point_cloud(T)
+        get_into(last, "x", out_x)
+        np.multiply(out_x.numpy() - htgt, 2.0 / n, out=seed.numpy())
+        last.set("grad_x", seed.numpy())
+        cg.compute_backward_pass(0)
+        get_into(l0, "grad_v", out_gv)
+        get_into(l0, "grad_F", out_gF)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    torch.cuda.synchronize(device)
+    ts = []
+    k = max(1, min(args.steps, 3))
+    for _ in range(k):
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    t = sum(ts)
+    return {"value": round(n * T * k / t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": round(1e3 * t / k, 3),
+            "path": "diffmpm_bindings.CompGraph (C ABI) from pinned host buffers"}
+
+
+def run_fp64(torch, dm, w, device, args):
+    """Plain all-FP64 GPU form on the first `fp64_steps` timesteps, and the
+    FP32 path's error against it on that rollout."""
+    T = min(w.steps, args.fp64_steps)
+    n = w.n
+    res = {}
+    grads = {}
+    for prec in ("fp64", "fp32"):
+        cg, keep = build_graph(dm, w, prec, w.checkpoint)
+        cg.set_up_comp_graph(T + 1)
+        tdt = torch.float64 if prec == "fp64" else torch.float32
+        tgt = torch.tensor(w.target, dtype=tdt, device=device)
+        stream = torch.cuda.current_stream(device)
+        cg.set_stream(stream)
+        device_rollout(torch, cg, T, tgt, n)  # warm-up
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        device_rollout(torch, cg, T, tgt, n)
+        e1.record(stream)
+        e1.synchronize()
+        res[prec] = n * T / (e0.elapsed_time(e1) / 1e3)
+        grads[prec] = {"x": cg.get_point_cloud(T).get("x", np.float64),
+                       "gv": cg.get_grad(0, "v", np.float64), "gF": cg.get_grad(0, "dFc", np.float64)}
+        del cg, keep
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
+    return {"value": round(res["fp64"], 1), "unit": UNIT, "timesteps": T,
+            "fp32_value_same_rollout": round(res["fp32"], 1), "speedup_fp32_vs_fp64": round(res["fp32"] / res["fp64"], 2),
+            "grad_v0_rel_err": rel(grads["fp32"]["gv"], grads["fp64"]["gv"]),
+            "grad_dFc_rel_err": rel(grads["fp32"]["gF"], grads["fp64"]["gF"]),
+            "x_T_max_abs_err": float(np.abs(grads["fp32"]["x"] - grads["fp64"]["x"]).max())}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_sample(w, particles: int, T: int):
+    import oracle as O
+    sel = slice(0, min(particles, w.n))
+    s = O.State(w.x[sel], w.v[sel], np.zeros((sel.stop, 3, 3)), w.F[sel], w.m[sel], w.vol[sel], w.lam[sel],
+                w.mu[sel])
+    g = O.Grid(w.dims, w.dx, w.grid_min)
+    prm = O.Params(dt=w.dt, drag=w.drag, smoothing=w.smoothing, exact=False)
+    seed = (2.0 / sel.stop) * (w.x[sel] - w.target[sel])
+    return s, g, prm, seed
+
+
+def cpu_baseline(w, args):
+    import build_oracle
+    build_oracle.build_oracle()
+    import oracle as O
+    orc = O.Oracle()
+    particles = args.cpu_particles or w.n
+    T = args.cpu_timesteps
+    s, g, prm, seed = cpu_sample(w, particles, T)
+    t0 = time.perf_counter()
+    orc.rollout(g, prm, s, T, seed)
+    dt = time.perf_counter() - t0
+    return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "kind": "port",
+            "sample": f"{s.n} of {w.n} particles of {w.name}, {T} timestep(s) forward + reference adjoint, "
+                      f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    w = make_workload(args.workload, args.quick)
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(w, args)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals)) if vals else cb["value"]
+    cb["value"] = round(v, 1)
+    return {"metric": METRIC, "value": round(v, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": w.name, "particles": w.n, "timesteps": w.steps,
+                       "note": "reference CPU path (restated in oracle/, OpenMP); each step is a bounded sample"},
+            "cpu_baseline": cb, "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+
+
+# ------------------------------------------------------------ distributed
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(torch, t, world, device):
+    if world == 1:
+        return t
+    import torch.distributed as dist
+    x = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="spheres2m", choices=["spheres2m", "ellipsoid64", "sphere32"])
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--cpu-particles", type=int, default=0, help="0: every particle")
+    ap.add_argument("--cpu-timesteps", type=int, default=2)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="reduced workload for smoke runs")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+        line = run_reference(args, rank, world)
+        if line:
+            print(json.dumps(line), flush=True)
+        return
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=device)
+    import build_oracle  # noqa: F401  (oracle build for the CPU baseline happens lazily)
+    line = run_ours(args, rank, world, device)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+/*
+ * mpm.h -- C ABI of libmpm.so, the GB300 (sm_103a) differentiable MPM engine.
+ *
+ * The entry points replace the reference's pybind11 module `diffmpm_bindings`
+ * (bind/bind.cpp:54-560) and the C++ classes it wraps (DiffMPMLib3D/
+ * PointCloud.h, Grid.h, CompGraph.h).  Each declaration cites the reference
+ * interface it stands in for.  Plain pointers and sizes only; no C++ or torch
+ * types cross this boundary, and nothing throws across it.
+ *
+ * Conventions
+ *   - Every function returns an int status: MPM_OK (0) or an MPM_ERR_* code;
+ *     mpm_last_error() returns a message for the calling thread's last error.
+ *   - Particle arrays are row-major: vectors (N,3), matrices (N,3,3).
+ *   - Grid arrays are flattened with node (i,j,k) at i*ny*nz + j*nz + k
+ *     (Grid.h:89-94).
+ *   - `dtype` arguments select MPM_DTYPE_F32 or MPM_DTYPE_F64 for the caller's
+ *     buffer; `on_device` says whether the buffer is CUDA device memory of the
+ *     current device (else host memory).
+ *   - Calls are synchronous with respect to the host unless stated otherwise;
+ *     work runs on the object's CUDA stream (mpm_compgraph_set_stream).
+ */
+#ifndef MPM_H
+#define MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+enum {
+    MPM_OK = 0,
+    MPM_ERR_ARG = 1,       /* invalid argument                      (RuntimeError) */
+    MPM_ERR_SHAPE = 2,     /* array shape / size mismatch           (RuntimeError) */
+    MPM_ERR_OOM = 3,       /* device allocation failed                              */
+    MPM_ERR_NONFINITE = 4, /* NaN/Inf detected in state or loss                     */
+    MPM_ERR_TIMEOUT = 5,   /* a bounded device wait gave up                         */
+    MPM_ERR_CUDA = 6,      /* CUDA runtime error                                    */
+    MPM_ERR_STATE = 7,     /* call not valid in the object's current state          */
+    MPM_ERR_RANGE = 8      /* index out of range                    (IndexError)    */
+};
+
+enum { MPM_FP32 = 0, MPM_FP64 = 1 };             /* engine precision            */
+enum { MPM_DTYPE_F32 = 0, MPM_DTYPE_F64 = 1 };   /* caller buffer element type  */
+enum { MPM_ADJ_REFERENCE = 0, MPM_ADJ_EXACT = 1 };
+enum { MPM_KERNEL_CUBIC = 0, MPM_KERNEL_QUADRATIC = 1 };
+enum { MPM_MAT_FCR = 0, MPM_MAT_NEOHOOKEAN = 1 };
+
+/* particle fields (MaterialPoint.h:17-46) */
+enum {
+    MPM_FIELD_X = 0,       /* (N,3)   position                                    */
+    MPM_FIELD_V = 1,       /* (N,3)   velocity                                    */
+    MPM_FIELD_F = 2,       /* (N,3,3) deformation gradient                        */
+    MPM_FIELD_C = 3,       /* (N,3,3) APIC affine matrix                          */
+    MPM_FIELD_DFC = 4,     /* (N,3,3) control dFc                                 */
+    MPM_FIELD_F_TOTAL = 5, /* (N,3,3) F + dFc (read only)                         */
+    MPM_FIELD_M = 6,       /* (N)     mass                                        */
+    MPM_FIELD_VOL = 7,     /* (N)     rest volume                                 */
+    MPM_FIELD_LAM = 8,     /* (N)     Lame lambda                                 */
+    MPM_FIELD_MU = 9,      /* (N)     Lame mu                                     */
+    MPM_FIELD_GRAD_X = 10, /* (N,3)   dL/dx                                       */
+    MPM_FIELD_GRAD_V = 11, /* (N,3)   dL/dv                                       */
+    MPM_FIELD_GRAD_F = 12, /* (N,3,3) dL/dF                                       */
+    MPM_FIELD_GRAD_C = 13, /* (N,3,3) dL/dC                                       */
+    MPM_FIELD_GRAD_DFC = 14,/* (N,3,3) dL/d(dFc), the control gradient (read only)*/
+    MPM_FIELD_GRAD_LAM = 15,/* (N)    dL/dlambda accumulated over the backward    */
+    MPM_FIELD_GRAD_MU = 16  /* (N)    dL/dmu accumulated over the backward        */
+};
+
+/* grid fields (GridNode.h:5-24) */
+enum { MPM_GRID_MASS = 0, MPM_GRID_MOMENTUM = 1, MPM_GRID_VELOCITY = 2 };
+
+/* simulation parameters; defaults = CompGraph's private members
+ * (CompGraph.h:78-83) and ForwardSimulation.cpp:13 */
+typedef struct mpm_params {
+    double dt;             /* 1/120 */
+    double drag;           /* 0.5   */
+    double smoothing;      /* 0.1   */
+    double f_ext[3];       /* 0     */
+    double bulk_viscosity; /* 0.25  */
+    double j_min;          /* 0.6 (trust region floor; <= 0 disables) */
+} mpm_params;
+
+typedef struct mpm_options {
+    int precision;        /* MPM_FP32 (FP32 with FP64 guard) or MPM_FP64 (plain all-FP64)  */
+    int adjoint;          /* MPM_ADJ_REFERENCE (term for term BackPropagation.cpp) or EXACT */
+    int kernel;           /* MPM_KERNEL_CUBIC (reference) or MPM_KERNEL_QUADRATIC           */
+    int material;         /* MPM_MAT_FCR (reference) or MPM_MAT_NEOHOOKEAN                  */
+    int checkpoint_every; /* 1: keep every layer (reference tape); k > 1: keep every k-th
+                             layer and recompute the others during the backward pass       */
+} mpm_options;
+
+/* OptInput (bind.cpp:30-52) -- the fields run_optimization reads */
+typedef struct mpm_opt_input {
+    int num_timesteps, control_stride, max_gd_iters, max_ls_iters, current_episodes;
+    double dt, drag, smoothing_factor, initial_alpha, gd_tol;
+    double f_ext[3];
+} mpm_opt_input;
+
+typedef struct mpm_pointcloud mpm_pointcloud;
+typedef struct mpm_grid mpm_grid;
+typedef struct mpm_compgraph mpm_compgraph;
+
+/* ------------------------------------------------------------------- misc */
+int mpm_version(void);
+const char* mpm_last_error(void);
+void mpm_default_params(mpm_params* p);
+void mpm_default_options(mpm_options* o);
+/* progress messages like the reference's std::cout lines (1 = on, default) */
+void mpm_set_verbose(int verbose);
+/* shared-memory node-tile budget of the scatter kernels (0 disables tiles) */
+int mpm_set_tile_nodes(int nodes);
+/* CalculateLameParameters (Elasticity.cpp:149-153; bind.cpp:540-544) */
+int mpm_lame(double young, double poisson, double* lam, double* mu);
+
+/* ------------------------------------------------------------- PointCloud */
+/* PointCloud with n particles: x = v = C = dFc = 0, F = I, m = vol = lam = mu = 0
+ * (MaterialPoint.h:17-31).  GeometryLoading.cpp:85-143 fills one from a mesh. */
+int mpm_pointcloud_create(int n, int precision, mpm_pointcloud** out);
+/* copy a field in (fields X..MU) */
+int mpm_pointcloud_set(mpm_pointcloud* pc, int field, const void* src, int dtype, int on_device);
+/* PointCloud::GetPoint* and bind.cpp:84-157 getters: copy a field out */
+int mpm_pointcloud_get(const mpm_pointcloud* pc, int field, void* dst, int dtype, int on_device);
+int mpm_pointcloud_size(const mpm_pointcloud* pc, int* n);
+int mpm_pointcloud_precision(const mpm_pointcloud* pc, int* precision);
+int mpm_pointcloud_release(mpm_pointcloud* pc);
+
+/* ------------------------------------------------------------------- Grid */
+/* Grid(int, int, int, float dx, Vec3 min) (Grid.cpp:7-26; bind.cpp:159-160) */
+int mpm_grid_create(int nx, int ny, int nz, double dx, const double* min_point, int precision, mpm_grid** out);
+int mpm_grid_info(const mpm_grid* g, int* dims, double* dx, double* min_point);
+/* Grid::GetNodeMasses / GetNodeVelocities (Grid.cpp:236-270) */
+int mpm_grid_get(const mpm_grid* g, int field, void* dst, int dtype, int on_device);
+int mpm_grid_set(mpm_grid* g, int field, const void* src, int dtype, int on_device);
+int mpm_grid_release(mpm_grid* g);
+
+/* P2G(pc, grid, 0, 0) into the un-reset grid (bind.cpp:546-549) */
+int mpm_p2g(mpm_pointcloud* pc, mpm_grid* g);
+/* CalculatePointCloudVolumes (ForwardSimulation.cpp:234-271; bind.cpp:551-554) */
+int mpm_calculate_point_cloud_volumes(mpm_pointcloud* pc, mpm_grid* g);
+
+/* -------------------------------------------------------------- CompGraph */
+/* CompGraph(pc, grid, target_grid) (CompGraph.cpp:21-28; bind.cpp:163-164):
+ * deep-copies pc and grid, keeps a reference to target_grid. opt may be NULL. */
+int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_grid* target_grid,
+                         const mpm_options* opt, mpm_compgraph** out);
+int mpm_compgraph_release(mpm_compgraph* cg);
+/* dt, drag, smoothing, f_ext (private in CompGraph.h:78-83; additive setter) */
+int mpm_compgraph_set_params(mpm_compgraph* cg, const mpm_params* p);
+int mpm_compgraph_get_params(const mpm_compgraph* cg, mpm_params* p);
+int mpm_compgraph_get_options(const mpm_compgraph* cg, mpm_options* o);
+/* run on a caller-owned cudaStream_t (NULL: the graph's own stream) */
+int mpm_compgraph_set_stream(mpm_compgraph* cg, void* stream);
+/* SetUpCompGraph (CompGraph.cpp:30-40; bind.cpp:345-347) */
+int mpm_compgraph_set_up(mpm_compgraph* cg, int num_layers);
+/* get_num_layers (bind.cpp:173-175) */
+int mpm_compgraph_num_layers(const mpm_compgraph* cg, int* out);
+/* ComputeForwardPass (CompGraph.cpp:131-141; bind.cpp:349-353) */
+int mpm_compgraph_forward(mpm_compgraph* cg, int start_layer, int episode);
+/* ComputeBackwardPass (CompGraph.cpp:143-211; bind.cpp:355-358) */
+int mpm_compgraph_backward(mpm_compgraph* cg, int control_layer);
+/* EndLayerMassLoss (CompGraph.cpp:42-129; bind.cpp:183-186) */
+int mpm_compgraph_mass_loss(mpm_compgraph* cg, double* loss);
+/* accumulate_render_grads (bind.cpp:189-279): float32 host arrays (n,3,3), (n,3) */
+int mpm_compgraph_accumulate_render_grads(mpm_compgraph* cg, const float* dLdF, const float* dLdx, int n);
+/* set/clear/has/info render gradients (bind.cpp:359-528) */
+int mpm_compgraph_set_render_gradients(mpm_compgraph* cg, const float* dLdF, const float* dLdx, int n);
+int mpm_compgraph_clear_render_gradients(mpm_compgraph* cg);
+int mpm_compgraph_render_gradient_info(const mpm_compgraph* cg, int* has, int* num_points, double* grad_F_norm,
+                                       double* grad_x_norm);
+/* get_point_cloud / get_point_cloud_at_timestep (bind.cpp:176-180,320-343): a live
+ * view of layer `layer`; release it with mpm_pointcloud_release */
+int mpm_compgraph_layer(mpm_compgraph* cg, int layer, mpm_pointcloud** out);
+/* promote_last_as_initial (bind.cpp:282-291) */
+int mpm_compgraph_promote_last_as_initial(mpm_compgraph* cg, int carry_grid);
+/* Compute_dLdF_Norm of a layer (PointCloud.cpp:24-35) over its control gradient */
+int mpm_compgraph_grad_norm(mpm_compgraph* cg, int layer, double* out);
+/* Descend_Adam on a layer's dFc (PointCloud.cpp:83-147), FP64 moments */
+int mpm_compgraph_adam_step(mpm_compgraph* cg, int layer, double alpha, double grad_norm, double beta1,
+                            double beta2, double eps, int timestep);
+/* OptimizeSingleTimestep (CompGraph.cpp:369-465; bind.cpp:294-317) */
+int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int timestep_idx, int max_gd_iters,
+                                           int current_episode, double initial_alpha, int max_line_search_iters);
+/* OptimizeDefGradControlSequence (CompGraph.cpp:213-368; bind.cpp:165-172) */
+int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt);
+/* number of grid nodes with mass > 0 in the forward grid of `layer` */
+int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long* out);
+/* number of grid nodes with mass > 0 in the forward grid of `layer` (the
+ * last forward step's grid when the graph is checkpointed) -- see above */
+
+/* ---------------------------------------------------------- measurement */
+/* kernel ids for the profiler */
+enum { MPM_K_P2G = 0, MPM_K_GRID_UPDATE = 1, MPM_K_G2P = 2, MPM_K_G2P_ADJ = 3, MPM_K_GRID_ADJ = 4,
+       MPM_K_P2G_ADJ = 5, MPM_K_LOSS = 6, MPM_K_ADAM = 7, MPM_K_NORM = 8, MPM_K_COUNT = 10 };
+/* record CUDA events around every kernel launch on its stream (1 = on) */
+int mpm_profile_enable(int on);
+int mpm_profile_reset(void);
+/* launches and summed device time of one kernel id since the last reset */
+int mpm_profile_query(int kernel, long long* launches, double* total_ms);
+const char* mpm_kernel_name(int kernel);
+/* number of engine kernels launched since the library was loaded */
+long long mpm_launch_count(void);
+
+/* accumulate dL/dlambda and dL/dmu per particle over the next backward
+ * passes; read them from the control layer's MPM_FIELD_GRAD_LAM/GRAD_MU */
+int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on);
+/* wait for all work queued on the graph's stream */
+int mpm_compgraph_synchronize(mpm_compgraph* cg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPM_H */

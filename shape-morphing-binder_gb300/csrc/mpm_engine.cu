@@ -1,0 +1,1564 @@
+// mpm_engine.cu -- host runtime of libmpm.so: PointCloud / Grid / CompGraph
+// objects over device memory, and the C ABI declared in include/mpm.h.
+//
+// The object model follows the reference (DiffMPMLib3D/PointCloud.h,
+// Grid.h, CompGraph.h, bind/bind.cpp): a CompGraph owns a tape of layers,
+// each a particle state plus the grid of the step that leaves it.  Particle
+// data lives on the GPU in structure-of-arrays planes (see mpm_launch.h);
+// every layer of one CompGraph shares the constant planes (m, vol, lam, mu).
+// With checkpoint_every = k > 1 only every k-th layer keeps its state and
+// the backward pass recomputes the others one segment at a time.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mpm.h"
+#include "mpm_launch.h"
+
+using namespace mpm;
+
+namespace {
+
+thread_local std::string g_err;
+int g_verbose = 1;
+// OptimizeSingleTimestep keeps a function-static Adam counter shared by every
+// CompGraph in the process (CompGraph.cpp:396); so does this library.
+int g_single_step_adam_t = 0;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Error(code, buf);
+}
+
+void ck(cudaError_t e, const char* what)
+{
+    if (e == cudaErrorMemoryAllocation) fail(MPM_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    if (e != cudaSuccess) fail(MPM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+template <typename F>
+int guard(F&& f)
+{
+    try {
+        f();
+        return MPM_OK;
+    } catch (const Error& e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return MPM_ERR_ARG;
+    }
+}
+
+void say(const char* fmt, ...)
+{
+    if (!g_verbose) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vfprintf(stdout, fmt, ap);
+    va_end(ap);
+    fflush(stdout);
+}
+
+// ----------------------------------------------------------------- profiler
+// Optional CUDA-event timing of every kernel the engine launches, recorded on
+// the stream the kernel runs on, plus a running launch counter.
+enum {
+    K_P2G = 0, K_GRID_UPDATE, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_LOSS, K_ADAM, K_NORM, K_AUX, K_COUNT
+};
+const char* k_names[K_COUNT] = {"p2g", "grid_update", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "mass_loss",
+                                "adam", "grad_norm", "aux"};
+// kernels each launcher issues (mass_loss: p2g, sums, nodes, gather)
+const int k_kernels[K_COUNT] = {1, 1, 1, 1, 1, 1, 4, 1, 1, 1};
+
+struct Prof {
+    bool on = false;
+    long long launches = 0;
+    struct Rec {
+        int id;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    long long count[K_COUNT] = {0};
+    double ms[K_COUNT] = {0};
+    cudaEvent_t get()
+    {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void resolve()
+    {
+        for (auto& r : pending) {
+            float t = 0;
+            cudaEventSynchronize(r.b);
+            cudaEventElapsedTime(&t, r.a, r.b);
+            ms[r.id] += t;
+            count[r.id] += 1;
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        pending.clear();
+    }
+} g_prof;
+
+struct KTimer {
+    int id;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    KTimer(int id_, cudaStream_t s_) : id(id_), s(s_)
+    {
+        g_prof.launches += k_kernels[id];
+        if (g_prof.on) {
+            a = g_prof.get();
+            cudaEventRecord(a, s);
+        }
+    }
+    ~KTimer()
+    {
+        if (a) {
+            cudaEvent_t b = g_prof.get();
+            cudaEventRecord(b, s);
+            g_prof.pending.push_back({id, a, b});
+            if (g_prof.pending.size() > 4096) g_prof.resolve();
+        }
+    }
+};
+
+// ------------------------------------------------------------ device memory
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t b) { alloc(b); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t b)
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = b;
+        if (b) ck(cudaMalloc(&p, b), "cudaMalloc");
+    }
+    template <typename T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+};
+using Buf = std::shared_ptr<DevBuf>;
+
+Buf make_buf(size_t bytes, cudaStream_t s, bool zero)
+{
+    auto b = std::make_shared<DevBuf>(bytes);
+    if (zero && bytes) ck(cudaMemsetAsync(b->p, 0, bytes, s), "cudaMemsetAsync");
+    return b;
+}
+
+long long pad_ld(int n) { return ((long long)n + 63) / 64 * 64; }
+size_t esize(int prec) { return prec == MPM_FP64 ? 8 : 4; }
+
+// --------------------------------------------------------------- particles
+
+// One particle set: the state planes, a shared reference to the constant
+// planes, the control planes and (lazily) gradients and Adam moments.
+struct PCData {
+    int n = 0;
+    long long ld = 0;
+    int prec = MPM_FP32;
+    Buf st;               // 24 planes
+    Buf co;               // 4 planes (shared between the layers of a graph)
+    Buf dfc;              // 9 planes; content valid only when !dfc_zero
+    bool dfc_zero = true;
+    Buf grads;            // 24 planes (lazy)
+    Buf gctl;             // 9 planes, control gradient (lazy; exact adjoint)
+    Buf glame;            // 2 planes, dL/dlam and dL/dmu (lazy)
+    Buf adam;             // 27 planes of double (lazy)
+    bool have_state = true;
+
+    size_t es() const { return esize(prec); }
+    size_t planes_bytes(int k) const { return (size_t)k * ld * es(); }
+    char* stp() const { return st ? st->as<char>() : nullptr; }
+};
+
+std::shared_ptr<PCData> new_pc(int n, int prec, cudaStream_t s)
+{
+    auto d = std::make_shared<PCData>();
+    d->n = n;
+    d->ld = pad_ld(n);
+    d->prec = prec;
+    d->st = make_buf(d->planes_bytes(ST_N), s, true);
+    d->co = make_buf(d->planes_bytes(CO_N), s, true);
+    d->dfc = make_buf(d->planes_bytes(9), s, false);
+    // F = I
+    for (int i = 0; i < 3; ++i) {
+        char* plane = d->stp() + (size_t)(ST_F + 4 * i) * d->ld * d->es();
+        if (prec == MPM_FP64) launch_fill_planes<double>(n, 1, d->ld, 1.0, (double*)plane, s);
+        else launch_fill_planes<float>(n, 1, d->ld, 1.0f, (float*)plane, s);
+    }
+    return d;
+}
+
+void copy_buf(const Buf& dst, const Buf& src, cudaStream_t s)
+{
+    ck(cudaMemcpyAsync(dst->p, src->p, src->bytes, cudaMemcpyDeviceToDevice, s), "cudaMemcpyAsync");
+}
+
+// deep copy (PointCloud copy constructor); constants stay shared unless asked
+std::shared_ptr<PCData> clone_pc(const PCData& a, cudaStream_t s, bool share_const)
+{
+    auto d = std::make_shared<PCData>();
+    d->n = a.n;
+    d->ld = a.ld;
+    d->prec = a.prec;
+    d->st = make_buf(a.st->bytes, s, false);
+    copy_buf(d->st, a.st, s);
+    if (share_const) {
+        d->co = a.co;
+    } else {
+        d->co = make_buf(a.co->bytes, s, false);
+        copy_buf(d->co, a.co, s);
+    }
+    d->dfc = make_buf(a.dfc->bytes, s, false);
+    d->dfc_zero = a.dfc_zero;
+    if (!a.dfc_zero) copy_buf(d->dfc, a.dfc, s);
+    if (a.grads) {
+        d->grads = make_buf(a.grads->bytes, s, false);
+        copy_buf(d->grads, a.grads, s);
+    }
+    if (a.adam) {
+        d->adam = make_buf(a.adam->bytes, s, false);
+        copy_buf(d->adam, a.adam, s);
+    }
+    return d;
+}
+
+void ensure_grads(PCData& d, cudaStream_t s)
+{
+    if (!d.grads) d.grads = make_buf(d.planes_bytes(ST_N), s, true);
+}
+
+void ensure_dfc_live(PCData& d, cudaStream_t s)
+{
+    if (d.dfc_zero) {
+        ck(cudaMemsetAsync(d.dfc->p, 0, d.dfc->bytes, s), "cudaMemsetAsync");
+        d.dfc_zero = false;
+    }
+}
+
+struct FieldDesc {
+    int plane;   // first plane
+    int k;       // components
+    int where;   // 0 state, 1 const, 2 dfc, 3 grads, 4 gctl, 5 ftotal, 6 glame
+};
+
+FieldDesc field_desc(int field)
+{
+    switch (field) {
+    case MPM_FIELD_X: return {ST_X, 3, 0};
+    case MPM_FIELD_V: return {ST_V, 3, 0};
+    case MPM_FIELD_F: return {ST_F, 9, 0};
+    case MPM_FIELD_C: return {ST_C, 9, 0};
+    case MPM_FIELD_DFC: return {0, 9, 2};
+    case MPM_FIELD_F_TOTAL: return {ST_F, 9, 5};
+    case MPM_FIELD_M: return {CO_M, 1, 1};
+    case MPM_FIELD_VOL: return {CO_VOL, 1, 1};
+    case MPM_FIELD_LAM: return {CO_LAM, 1, 1};
+    case MPM_FIELD_MU: return {CO_MU, 1, 1};
+    case MPM_FIELD_GRAD_X: return {ST_X, 3, 3};
+    case MPM_FIELD_GRAD_V: return {ST_V, 3, 3};
+    case MPM_FIELD_GRAD_F: return {ST_F, 9, 3};
+    case MPM_FIELD_GRAD_C: return {ST_C, 9, 3};
+    case MPM_FIELD_GRAD_DFC: return {0, 9, 4};
+    case MPM_FIELD_GRAD_LAM: return {0, 1, 6};
+    case MPM_FIELD_GRAD_MU: return {1, 1, 6};
+    default: fail(MPM_ERR_ARG, "unknown particle field %d", field);
+    }
+}
+
+// Grow-only device staging buffer for host<->device copies (per host thread;
+// every host-side copy completes before the call returns).
+DevBuf& staging(size_t bytes)
+{
+    static thread_local DevBuf buf;
+    if (buf.bytes < bytes) buf.alloc(bytes + bytes / 4);
+    return buf;
+}
+
+// Convert between a caller buffer (row-major, dtype, host/device) and planes.
+template <typename R>
+void planes_in(int n, int k, long long ld, const void* src, int dtype, int on_device, R* dst, cudaStream_t s)
+{
+    if (n == 0) return;
+    const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
+    const size_t bytes = (size_t)n * k * tsz;
+    const void* dsrc = src;
+    if (!on_device) {
+        DevBuf& tmp = staging(bytes);
+        ck(cudaMemcpyAsync(tmp.p, src, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
+        dsrc = tmp.p;
+    }
+    if (dtype == MPM_DTYPE_F64) launch_aos_to_planes<R, double>(n, k, ld, (const double*)dsrc, dst, s);
+    else launch_aos_to_planes<R, float>(n, k, ld, (const float*)dsrc, dst, s);
+    ck(cudaGetLastError(), "aos_to_planes");
+    if (!on_device) ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+template <typename R>
+void planes_out(int n, int k, long long ld, const R* src, void* dst, int dtype, int on_device, cudaStream_t s)
+{
+    if (n == 0) return;
+    const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
+    const size_t bytes = (size_t)n * k * tsz;
+    void* ddst = dst;
+    DevBuf* tmp = nullptr;
+    if (!on_device) {
+        tmp = &staging(bytes);
+        ddst = tmp->p;
+    }
+    if (dtype == MPM_DTYPE_F64) launch_planes_to_aos<R, double>(n, k, ld, src, (double*)ddst, s);
+    else launch_planes_to_aos<R, float>(n, k, ld, src, (float*)ddst, s);
+    ck(cudaGetLastError(), "planes_to_aos");
+    if (!on_device) {
+        ck(cudaMemcpyAsync(dst, tmp->p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
+        ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+}
+
+template <typename R>
+void pc_get(const PCData& d, int field, void* dst, int dtype, int on_device, cudaStream_t s)
+{
+    FieldDesc f = field_desc(field);
+    const long long ld = d.ld;
+    const R* base = nullptr;
+    DevBuf tmp;
+    switch (f.where) {
+    case 0:
+        if (!d.have_state) fail(MPM_ERR_STATE, "layer state is not stored (checkpointed graph)");
+        base = d.st->as<R>() + f.plane * ld;
+        break;
+    case 1: base = d.co->as<R>() + f.plane * ld; break;
+    case 2:
+    case 4:
+    case 6: {
+        const Buf& b = f.where == 2 ? d.dfc : (f.where == 4 ? (d.gctl ? d.gctl : d.grads) : d.glame);
+        bool zero = (f.where == 2 && d.dfc_zero) || !b;
+        if (zero) {
+            tmp.alloc((size_t)f.k * ld * sizeof(R));
+            ck(cudaMemsetAsync(tmp.p, 0, tmp.bytes, s), "memset");
+            base = tmp.as<R>();
+        } else {
+            base = b->as<R>() + (f.where == 4 && !d.gctl ? ST_F * ld : f.plane * ld);
+        }
+        break;
+    }
+    case 3:
+        if (!d.grads) {
+            tmp.alloc((size_t)f.k * ld * sizeof(R));
+            ck(cudaMemsetAsync(tmp.p, 0, tmp.bytes, s), "memset");
+            base = tmp.as<R>();
+        } else {
+            base = d.grads->as<R>() + f.plane * ld;
+        }
+        break;
+    case 5:
+        if (!d.have_state) fail(MPM_ERR_STATE, "layer state is not stored (checkpointed graph)");
+        tmp.alloc((size_t)9 * ld * sizeof(R));
+        ck(cudaMemcpyAsync(tmp.p, d.st->as<R>() + ST_F * ld, tmp.bytes, cudaMemcpyDeviceToDevice, s), "copy");
+        if (!d.dfc_zero) launch_axpy_planes<R>(d.n, 9, ld, R(1), d.dfc->as<R>(), tmp.as<R>(), s);
+        base = tmp.as<R>();
+        break;
+    }
+    planes_out<R>(d.n, f.k, ld, base, dst, dtype, on_device, s);
+}
+
+template <typename R>
+void pc_set(PCData& d, int field, const void* src, int dtype, int on_device, cudaStream_t s)
+{
+    FieldDesc f = field_desc(field);
+    R* base = nullptr;
+    switch (f.where) {
+    case 0: base = d.st->as<R>() + f.plane * d.ld; break;
+    case 1: base = d.co->as<R>() + f.plane * d.ld; break;
+    case 2:
+        d.dfc_zero = false;
+        base = d.dfc->as<R>();
+        break;
+    case 3:
+        ensure_grads(d, s);
+        base = d.grads->as<R>() + f.plane * d.ld;
+        break;
+    default: fail(MPM_ERR_ARG, "field %d is read only", field);
+    }
+    planes_in<R>(d.n, f.k, d.ld, src, dtype, on_device, base, s);
+}
+
+// ------------------------------------------------------------------- grids
+
+struct GridData {
+    int dims[3] = {0, 0, 0};
+    double dx = 1.0;
+    double gmin[3] = {0, 0, 0};
+    int prec = MPM_FP32;
+    Buf nodes;  // 4 scalars per node
+    long long nn() const { return (long long)dims[0] * dims[1] * dims[2]; }
+};
+
+StepCfg base_cfg(const GridData& g)
+{
+    StepCfg c;
+    for (int a = 0; a < 3; ++a) {
+        c.dims[a] = g.dims[a];
+        c.gmin[a] = g.gmin[a];
+    }
+    c.dx = g.dx;
+    return c;
+}
+
+template <typename R>
+void grid_get(const GridData& g, int field, void* dst, int dtype, int on_device, cudaStream_t s)
+{
+    const long long nn = g.nn();
+    const R* src = g.nodes->as<R>();
+    // node layout (p0,p1,p2,m): gather with a plane view of stride 1 over 4*nn
+    // by treating the array as (nn,4) row-major
+    DevBuf tmp(sizeof(R) * 4 * nn);
+    ck(cudaMemcpyAsync(tmp.p, src, tmp.bytes, cudaMemcpyDeviceToDevice, s), "copy");
+    std::vector<R> h(4 * (size_t)nn);
+    ck(cudaMemcpyAsync(h.data(), tmp.p, tmp.bytes, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    const int k = field == MPM_GRID_MASS ? 1 : 3;
+    const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
+    std::vector<char> out((size_t)nn * k * tsz);
+    for (long long i = 0; i < nn; ++i) {
+        for (int q = 0; q < k; ++q) {
+            double v = field == MPM_GRID_MASS ? (double)h[4 * i + 3] : (double)h[4 * i + q];
+            if (field == MPM_GRID_VELOCITY) v = 0;  // velocities are not kept on standalone grids
+            if (dtype == MPM_DTYPE_F64) ((double*)out.data())[i * k + q] = v;
+            else ((float*)out.data())[i * k + q] = (float)v;
+        }
+    }
+    if (on_device) ck(cudaMemcpy(dst, out.data(), out.size(), cudaMemcpyHostToDevice), "H2D");
+    else memcpy(dst, out.data(), out.size());
+}
+
+template <typename R>
+void grid_set(GridData& g, int field, const void* src, int dtype, int on_device, cudaStream_t s)
+{
+    const long long nn = g.nn();
+    const int k = field == MPM_GRID_MASS ? 1 : 3;
+    const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
+    std::vector<char> in((size_t)nn * k * tsz);
+    if (on_device) ck(cudaMemcpy(in.data(), src, in.size(), cudaMemcpyDeviceToHost), "D2H");
+    else memcpy(in.data(), src, in.size());
+    std::vector<R> h(4 * (size_t)nn);
+    ck(cudaMemcpyAsync(h.data(), g.nodes->p, g.nodes->bytes, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    for (long long i = 0; i < nn; ++i)
+        for (int q = 0; q < k; ++q) {
+            double v = dtype == MPM_DTYPE_F64 ? ((double*)in.data())[i * k + q] : ((float*)in.data())[i * k + q];
+            h[4 * i + (field == MPM_GRID_MASS ? 3 : q)] = (R)v;
+        }
+    ck(cudaMemcpyAsync(g.nodes->p, h.data(), g.nodes->bytes, cudaMemcpyHostToDevice, s), "H2D");
+    ck(cudaStreamSynchronize(s), "sync");
+}
+
+// --------------------------------------------------------------- CompGraph
+
+struct Layer {
+    std::shared_ptr<PCData> pc;  // null for non-stored layers of a checkpointed graph
+    Buf grid;                    // grid of the step leaving this layer (lazy)
+    Buf trust;                   // trust-region scale of that step (exact adjoint)
+};
+
+struct Graph {
+    int prec = MPM_FP32;
+    mpm_options opt{};
+    mpm_params prm{};
+    GridData geom;                      // copy of the construction grid's geometry
+    std::shared_ptr<GridData> target;   // aliased target grid
+    std::shared_ptr<PCData> base;       // template for layer construction
+    std::vector<Layer> layers;
+    cudaStream_t own = nullptr, stream = nullptr;
+    // scratch
+    Buf adj, lgm, ldm, acc;
+    Buf fgrid, ftrust;                              // checkpointed forward
+    std::shared_ptr<PCData> ping, pong;             // non-stored forward states
+    std::vector<std::shared_ptr<PCData>> seg;       // recomputed segment states
+    std::vector<Buf> sgrid, strust;                 // recomputed segment grids
+    bool lame_on = false;                           // accumulate dL/dlam, dL/dmu
+    Buf glame;                                      // 2 planes
+    // render gradients (stored on the host like CompGraph.h:73-76)
+    std::vector<float> rgF, rgx;
+    bool has_rg = false;
+    size_t rg_n = 0;
+
+    ~Graph()
+    {
+        if (own) cudaStreamDestroy(own);
+    }
+
+    int n() const { return base->n; }
+    long long ld() const { return base->ld; }
+
+    StepCfg cfg() const
+    {
+        StepCfg c = base_cfg(geom);
+        c.dt = prm.dt;
+        c.drag = prm.drag;
+        c.smoothing = prm.smoothing;
+        for (int a = 0; a < 3; ++a) c.fext[a] = prm.f_ext[a];
+        c.bulk = prm.bulk_viscosity;
+        c.jmin = prm.j_min;
+        c.kernel = opt.kernel;
+        c.material = opt.material;
+        c.exact = opt.adjoint == MPM_ADJ_EXACT;
+        return c;
+    }
+
+    bool stored(int i) const
+    {
+        const int k = opt.checkpoint_every;
+        const int L = (int)layers.size();
+        return k <= 1 || i % k == 0 || i == L - 1;
+    }
+};
+
+}  // namespace
+
+struct mpm_pointcloud {
+    std::shared_ptr<PCData> d;
+    cudaStream_t stream = nullptr;
+};
+struct mpm_grid {
+    std::shared_ptr<GridData> d;
+};
+struct mpm_compgraph {
+    Graph g;
+};
+
+namespace {
+
+template <typename Fn>
+void with_prec(int prec, Fn&& fn)
+{
+    if (prec == MPM_FP64) fn(double(0));
+    else fn(float(0));
+}
+
+void check_launch(const char* what) { ck(cudaGetLastError(), what); }
+
+Buf& ensure(Buf& b, size_t bytes, cudaStream_t s, bool zero)
+{
+    if (!b || b->bytes < bytes) b = make_buf(bytes, s, zero);
+    return b;
+}
+
+// One forward step: layer i -> layer i+1 (ForwardSimulation.cpp:159-185)
+template <typename R>
+void step_forward(const StepCfg& c, PCData& a, PCData& b, Buf& grid, Buf& trust, cudaStream_t s)
+{
+    const long long nn = c.nodes();
+    ensure(grid, sizeof(R) * 4 * nn, s, false);
+    ck(cudaMemsetAsync(grid->p, 0, sizeof(R) * 4 * nn, s), "grid reset");
+    const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
+    {
+        KTimer kt(K_P2G, s);
+        launch_p2g<R>(c, a.n, a.ld, a.st->as<R>(), dfc, a.co->as<R>(), grid->as<R>(), s);
+    }
+    check_launch("p2g");
+    {
+        KTimer kt(K_GRID_UPDATE, s);
+        launch_grid_update<R>(c, grid->as<R>(), s);
+    }
+    check_launch("grid_update");
+    R* tr = nullptr;
+    if (c.exact) tr = ensure(trust, sizeof(R) * a.ld, s, false)->as<R>();
+    {
+        KTimer kt(K_G2P, s);
+        launch_g2p<R>(c, a.n, a.ld, a.st->as<R>(), dfc, grid->as<R>(), b.st->as<R>(), tr, s);
+    }
+    check_launch("g2p");
+    b.dfc_zero = true;
+    b.have_state = true;
+}
+
+// One adjoint step: grads of layer i+1 -> grads of layer i (BackPropagation.cpp:9-144)
+template <typename R>
+void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& grid, const Buf& trust,
+                   cudaStream_t s)
+{
+    const long long nn = c.nodes();
+    if (!grid) fail(MPM_ERR_STATE, "backward pass before the forward pass of this step");
+    ensure(G.adj, sizeof(R) * 4 * nn, s, false);
+    ck(cudaMemsetAsync(G.adj->p, 0, sizeof(R) * 4 * nn, s), "adj reset");
+    ensure_grads(a, s);
+    ensure_grads(b, s);
+    const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
+    const R* tr = (c.exact && trust) ? trust->as<R>() : nullptr;
+    {
+        KTimer kt(K_G2P_ADJ, s);
+        launch_g2p_adj<R>(c, a.n, a.ld, a.st->as<R>(), dfc, b.st->as<R>(), b.grads->as<R>(), tr, G.adj->as<R>(), s);
+    }
+    check_launch("g2p_adj");
+    {
+        KTimer kt(K_GRID_ADJ, s);
+        launch_grid_adj<R>(c, grid->as<R>(), G.adj->as<R>(), s);
+    }
+    check_launch("grid_adj");
+    R* gctl = nullptr;
+    if (c.exact) gctl = ensure(a.gctl, a.planes_bytes(9), s, false)->as<R>();
+    R *glam = nullptr, *gmu = nullptr;
+    if (G.lame_on && G.glame) {
+        glam = G.glame->as<R>();
+        gmu = glam + a.ld;
+    }
+    {
+        KTimer kt(K_P2G_ADJ, s);
+        launch_p2g_adj<R>(c, a.n, a.ld, a.st->as<R>(), dfc, a.co->as<R>(), b.st->as<R>(), b.grads->as<R>(), tr,
+                          grid->as<R>(), G.adj->as<R>(), a.grads->as<R>(), gctl, glam, gmu, s);
+    }
+    check_launch("p2g_adj");
+}
+
+std::shared_ptr<PCData> shell_like(const PCData& a, cudaStream_t s, bool with_state)
+{
+    auto d = std::make_shared<PCData>();
+    d->n = a.n;
+    d->ld = a.ld;
+    d->prec = a.prec;
+    d->co = a.co;
+    if (with_state) d->st = make_buf(a.planes_bytes(ST_N), s, false);
+    d->dfc = make_buf(a.planes_bytes(9), s, false);
+    d->dfc_zero = true;
+    d->have_state = with_state;
+    return d;
+}
+
+// ComputeForwardPass (CompGraph.cpp:131-141).  With checkpointing the
+// non-stored layers pass through two scratch states and one scratch grid.
+template <typename R>
+void graph_forward(Graph& G, int start)
+{
+    const int L = (int)G.layers.size();
+    if (start < 0 || start >= L) fail(MPM_ERR_RANGE, "start layer %d out of range [0, %d)", start, L);
+    cudaStream_t s = G.stream;
+    StepCfg c = G.cfg();
+    const bool full = G.opt.checkpoint_every <= 1;
+    if (!G.layers[start].pc || !G.layers[start].pc->have_state)
+        fail(MPM_ERR_STATE, "layer %d is not stored; forward passes of a checkpointed graph start at a stored layer",
+             start);
+    PCData* cur = G.layers[start].pc.get();
+    for (int i = start; i < L - 1; ++i) {
+        PCData* nxt;
+        if (G.stored(i + 1)) {
+            nxt = G.layers[i + 1].pc.get();
+            if (!nxt->st) nxt->st = make_buf(cur->planes_bytes(ST_N), s, false);
+        } else {
+            auto& tmp = (cur == G.ping.get()) ? G.pong : G.ping;
+            if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
+            nxt = tmp.get();
+        }
+        if (full) step_forward<R>(c, *cur, *nxt, G.layers[i].grid, G.layers[i].trust, s);
+        else step_forward<R>(c, *cur, *nxt, G.fgrid, G.ftrust, s);
+        cur = nxt;
+    }
+}
+
+template <typename R>
+void inject_render_grads(Graph& G)
+{
+    if (!G.has_rg || G.layers.empty()) return;
+    PCData& last = *G.layers.back().pc;
+    if (G.rg_n != (size_t)last.n) {
+        fprintf(stderr, "[WARN] Render gradient size mismatch: stored %zu but layer has %d points. Skipping injection.\n",
+                G.rg_n, last.n);
+        return;
+    }
+    say("[C++] Injecting render gradients to layer %d (%d points)\n", (int)G.layers.size() - 1, last.n);
+    cudaStream_t s = G.stream;
+    ensure_grads(last, s);
+    DevBuf tmp((size_t)12 * last.ld * sizeof(R));
+    planes_in<R>(last.n, 9, last.ld, G.rgF.data(), MPM_DTYPE_F32, 0, tmp.as<R>(), s);
+    planes_in<R>(last.n, 3, last.ld, G.rgx.data(), MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s);
+    launch_axpy_planes<R>(last.n, 9, last.ld, R(1), tmp.as<R>(), last.grads->as<R>() + ST_F * last.ld, s);
+    launch_axpy_planes<R>(last.n, 3, last.ld, R(1), tmp.as<R>() + 9 * last.ld, last.grads->as<R>() + ST_X * last.ld,
+                          s);
+    check_launch("inject");
+    ck(cudaStreamSynchronize(s), "sync");
+    say("[C++] Render gradients injected (L_tot = L_phys + L_render)\n");
+}
+
+// ComputeBackwardPass (CompGraph.cpp:143-211).  With checkpointing each
+// segment [lo, hi] between stored layers is recomputed from lo (states, grids
+// and trust scales into segment scratch) and then run backwards.
+template <typename R>
+void graph_backward(Graph& G, int control)
+{
+    const int L = (int)G.layers.size();
+    if (control < 0 || control >= L) fail(MPM_ERR_RANGE, "control layer %d out of range [0, %d)", control, L);
+    cudaStream_t s = G.stream;
+    inject_render_grads<R>(G);
+    StepCfg c = G.cfg();
+    const int k = std::max(1, G.opt.checkpoint_every);
+    if (G.lame_on) {
+        PCData& ctl = *G.layers[control].pc;
+        G.glame = make_buf(ctl.planes_bytes(2), s, true);
+        ctl.glame = G.glame;
+    }
+    if (k == 1) {
+        for (int i = L - 2; i >= control; --i) {
+            Layer& la = G.layers[i];
+            step_backward<R>(G, c, *la.pc, *G.layers[i + 1].pc, la.grid, la.trust, s);
+        }
+        return;
+    }
+    if (!G.stored(control)) fail(MPM_ERR_STATE, "control layer %d is not a stored layer of the checkpointed graph", control);
+    int hi = L - 1;
+    while (hi > control) {
+        const int lo = ((hi - 1) / k) * k;
+        const int cnt = hi - lo + 1;
+        if ((int)G.seg.size() < cnt) G.seg.resize(cnt);
+        if ((int)G.sgrid.size() < cnt) {
+            G.sgrid.resize(cnt);
+            G.strust.resize(cnt);
+        }
+        std::vector<PCData*> S(cnt);
+        S[0] = G.layers[lo].pc.get();
+        S[cnt - 1] = G.layers[hi].pc.get();
+        for (int j = 1; j < cnt - 1; ++j) {
+            if (!G.seg[j] || G.seg[j]->n != S[0]->n) G.seg[j] = shell_like(*S[0], s, true);
+            S[j] = G.seg[j].get();
+        }
+        if (!G.ping || G.ping->n != S[0]->n) G.ping = shell_like(*S[0], s, true);
+        for (int j = 0; j < cnt - 1; ++j) {
+            PCData* out = (j + 1 < cnt - 1) ? S[j + 1] : G.ping.get();
+            step_forward<R>(c, *S[j], *out, G.sgrid[j], G.strust[j], s);
+        }
+        const int stop = std::max(control, lo);
+        for (int i = hi - 1; i >= stop; --i) {
+            const int j = i - lo;
+            step_backward<R>(G, c, *S[j], *S[j + 1], G.sgrid[j], G.strust[j], s);
+        }
+        hi = lo;
+    }
+}
+
+template <typename R>
+double graph_loss(Graph& G)
+{
+    if (!G.target) fail(MPM_ERR_STATE, "CompGraph has no target grid");
+    if (G.target->prec != G.prec) fail(MPM_ERR_ARG, "target grid precision differs from the graph's");
+    for (int a = 0; a < 3; ++a)
+        if (G.target->dims[a] != G.geom.dims[a]) fail(MPM_ERR_SHAPE, "target grid dims differ from the graph grid");
+    cudaStream_t s = G.stream;
+    PCData& last = *G.layers.back().pc;
+    if (!last.have_state) fail(MPM_ERR_STATE, "last layer not stored");
+    ensure_grads(last, s);
+    StepCfg c = G.cfg();
+    const long long nn = c.nodes();
+    ensure(G.lgm, sizeof(R) * nn, s, false);
+    ensure(G.ldm, sizeof(R) * nn, s, false);
+    ensure(G.acc, sizeof(double) * 8, s, true);
+    {
+        KTimer kt(K_LOSS, s);
+        launch_loss<R>(c, last.n, last.ld, last.st->as<R>(), last.co->as<R>(), G.target->nodes->as<R>(),
+                       G.lgm->as<R>(), G.ldm->as<R>(), G.acc->as<double>(), last.grads->as<R>(), s);
+    }
+    check_launch("loss");
+    double acc[4];
+    ck(cudaMemcpyAsync(acc, G.acc->p, sizeof acc, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    return acc[2];
+}
+
+template <typename R>
+double graph_grad_norm(Graph& G, int layer)
+{
+    PCData& d = *G.layers.at(layer).pc;
+    cudaStream_t s = G.stream;
+    ensure(G.acc, sizeof(double) * 8, s, true);
+    if (!d.grads) return 0.0;
+    const R* g = d.gctl ? d.gctl->as<R>() : d.grads->as<R>() + ST_F * d.ld;
+    {
+        KTimer kt(K_NORM, s);
+        launch_sumsq<R>(d.n, d.ld, g, 0, 9, G.acc->as<double>(), s);
+    }
+    check_launch("sumsq");
+    double v;
+    ck(cudaMemcpyAsync(&v, G.acc->p, sizeof v, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    return std::sqrt(v);
+}
+
+template <typename R>
+void graph_adam(Graph& G, int layer, double alpha, double gnorm, double b1, double b2, double eps, int t)
+{
+    PCData& d = *G.layers.at(layer).pc;
+    cudaStream_t s = G.stream;
+    ensure_grads(d, s);
+    ensure_dfc_live(d, s);
+    if (!d.adam) d.adam = make_buf(sizeof(double) * 27 * d.ld, s, true);
+    const R* g = d.gctl ? d.gctl->as<R>() : d.grads->as<R>() + ST_F * d.ld;
+    double* m = d.adam->as<double>();
+    const double inv_gn = 1.0 / std::max(gnorm, 1e-12);
+    {
+        KTimer kt(K_ADAM, s);
+        launch_adam<R>(d.n, d.ld, g, d.dfc->as<R>(), m, m + 9 * d.ld, m + 18 * d.ld, alpha, inv_gn, b1, b2, eps,
+                       std::max(1, t), s);
+    }
+    check_launch("adam");
+}
+
+// backup/restore of dFc and the Adam moments of one layer (line search)
+struct Backup {
+    Buf dfc, adam;
+    bool dfc_zero = true, had_adam = false;
+};
+
+void backup(PCData& d, Backup& b, cudaStream_t s)
+{
+    b.dfc_zero = d.dfc_zero;
+    if (!d.dfc_zero) {
+        ensure(b.dfc, d.dfc->bytes, s, false);
+        copy_buf(b.dfc, d.dfc, s);
+    }
+    b.had_adam = (bool)d.adam;
+    if (d.adam) {
+        ensure(b.adam, d.adam->bytes, s, false);
+        copy_buf(b.adam, d.adam, s);
+    }
+}
+
+void restore(PCData& d, Backup& b, cudaStream_t s)
+{
+    d.dfc_zero = b.dfc_zero;
+    if (!b.dfc_zero) ck(cudaMemcpyAsync(d.dfc->p, b.dfc->p, d.dfc->bytes, cudaMemcpyDeviceToDevice, s), "restore");
+    if (b.had_adam) ck(cudaMemcpyAsync(d.adam->p, b.adam->p, d.adam->bytes, cudaMemcpyDeviceToDevice, s), "restore");
+    else d.adam.reset();
+}
+
+template <typename R>
+void graph_set_up(Graph& G, int num_layers)
+{
+    if (num_layers <= 0) fail(MPM_ERR_ARG, "num_layers must be positive");
+    cudaStream_t s = G.stream;
+    G.layers.resize(num_layers);
+    for (int i = 1; i < num_layers; ++i) {
+        if (G.stored(i)) {
+            G.layers[i].pc = clone_pc(*G.layers[0].pc, s, true);
+        } else {
+            G.layers[i].pc = shell_like(*G.layers[0].pc, s, false);
+        }
+        G.layers[i].grid.reset();
+        G.layers[i].trust.reset();
+    }
+}
+
+template <typename R>
+void graph_optimize_single(Graph& G, int t, int max_gd, int episode, double alpha0, int max_ls)
+{
+    (void)episode;
+    const int L = (int)G.layers.size();
+    if (t < 0 || t >= L - 1) {
+        fprintf(stderr, "Invalid timestep index: %d\n", t);
+        return;
+    }
+    say("Optimizing single timestep: %d (alpha=%g)\n", t, alpha0);
+    cudaStream_t s = G.stream;
+    const double beta1 = 0.9, beta2 = 0.999, eps = 1e-3;
+    double alpha = alpha0;
+    Backup bk;
+    for (int it = 0; it < max_gd; ++it) {
+        graph_forward<R>(G, t);
+        double loss = graph_loss<R>(G);
+        if (!std::isfinite(loss)) {
+            say("Warning: Non-finite loss. Aborting.\n");
+            break;
+        }
+        graph_backward<R>(G, t);
+        PCData& pc = *G.layers[t].pc;
+        double gn = std::max(graph_grad_norm<R>(G, t), 1e-12);
+        backup(pc, bk, s);
+        bool ok = false;
+        double a = alpha;
+        for (int ls = 0; ls < max_ls; ++ls) {
+            graph_adam<R>(G, t, a, gn, beta1, beta2, eps, g_single_step_adam_t + 1);
+            graph_forward<R>(G, t);
+            double nl = graph_loss<R>(G);
+            if (std::isfinite(nl) && nl < loss) {
+                ++g_single_step_adam_t;
+                alpha = std::min(a * 1.1, alpha0);
+                ok = true;
+                say("  Step accepted at ls_iter=%d, loss=%g\n", ls, nl);
+                break;
+            }
+            restore(pc, bk, s);
+            a *= 0.5;
+        }
+        if (!ok) {
+            say("  Line search failed.\n");
+            break;
+        }
+    }
+}
+
+template <typename R>
+void graph_run_optimization(Graph& G, const mpm_opt_input& o)
+{
+    G.prm.dt = o.dt;
+    G.prm.drag = o.drag;
+    G.prm.smoothing = o.smoothing_factor;
+    for (int a = 0; a < 3; ++a) G.prm.f_ext[a] = o.f_ext[a];
+    say("Optimizing with num_steps=%d, dt=%g, drag=%g\n", o.num_timesteps, o.dt, o.drag);
+    graph_set_up<R>(G, o.num_timesteps);
+    graph_forward<R>(G, 0);
+    double init_loss = graph_loss<R>(G);
+    say("Initial loss = %g\n", init_loss);
+    graph_backward<R>(G, 0);
+    say("Initial global gradient norm = %g\n", graph_grad_norm<R>(G, 0));
+    const double beta1 = 0.9, beta2 = 0.999, eps = 1e-3;
+    int adam_t = 0;
+    cudaStream_t s = G.stream;
+    Backup bk;
+    const int passes = 3;
+    say("Number of Iteration Passes: %d\n", passes);
+    for (int pass = 0; pass < passes; ++pass) {
+        for (int ct = 0; ct < o.num_timesteps - 1; ct += std::max(1, o.control_stride)) {
+            say("Optimizing for control timestep: %d (Pass %d)\n", ct, pass + 1);
+            double alpha = o.initial_alpha, init_norm = 0;
+            for (int it = 0; it < o.max_gd_iters; ++it) {
+                graph_forward<R>(G, ct);
+                double loss = graph_loss<R>(G);
+                if (!std::isfinite(loss)) {
+                    say("Warning: Non-finite loss detected. Aborting step.\n");
+                    break;
+                }
+                graph_backward<R>(G, ct);
+                double gn = std::max(graph_grad_norm<R>(G, ct), 1e-12);
+                if (it == 0) init_norm = gn;
+                if (gn < o.gd_tol * init_norm) {
+                    say("Converged at GD iteration %d.\n", it);
+                    break;
+                }
+                PCData& pc = *G.layers[ct].pc;
+                backup(pc, bk, s);
+                bool ok = false;
+                double a = alpha;
+                for (int ls = 0; ls < o.max_ls_iters; ++ls) {
+                    graph_adam<R>(G, ct, a, gn, beta1, beta2, eps, adam_t + 1);
+                    graph_forward<R>(G, ct);
+                    double nl = graph_loss<R>(G);
+                    if (std::isfinite(nl) && nl < loss) {
+                        ++adam_t;
+                        alpha = std::min(a * 1.1, o.initial_alpha);
+                        ok = true;
+                        break;
+                    }
+                    restore(pc, bk, s);
+                    a *= 0.5;
+                }
+                if (!ok) {
+                    say("Line search failed. Moving to next control step.\n");
+                    break;
+                }
+            }
+        }
+    }
+    say("Final loss = %g\n", graph_loss<R>(G));
+    say("Optimization finished.\n");
+}
+
+void check_pc(const mpm_pointcloud* pc)
+{
+    if (!pc || !pc->d) fail(MPM_ERR_ARG, "PointCloud is null.");
+}
+void check_grid(const mpm_grid* g)
+{
+    if (!g || !g->d) fail(MPM_ERR_ARG, "Grid is null.");
+}
+void check_cg(const mpm_compgraph* cg)
+{
+    if (!cg) fail(MPM_ERR_ARG, "CompGraph is null.");
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+int mpm_version(void) { return 100; }
+
+const char* mpm_last_error(void) { return g_err.c_str(); }
+
+void mpm_default_params(mpm_params* p)
+{
+    if (!p) return;
+    p->dt = 1.0 / 120.0;
+    p->drag = 0.5;
+    p->smoothing = 0.1;
+    p->f_ext[0] = p->f_ext[1] = p->f_ext[2] = 0.0;
+    p->bulk_viscosity = 0.25;
+    p->j_min = 0.6;
+}
+
+void mpm_default_options(mpm_options* o)
+{
+    if (!o) return;
+    o->precision = MPM_FP32;
+    o->adjoint = MPM_ADJ_REFERENCE;
+    o->kernel = MPM_KERNEL_CUBIC;
+    o->material = MPM_MAT_FCR;
+    o->checkpoint_every = 1;
+}
+
+void mpm_set_verbose(int v) { g_verbose = v; }
+
+int mpm_set_tile_nodes(int nodes)
+{
+    return guard([&] {
+        if (nodes < 0 || nodes > 2816) fail(MPM_ERR_ARG, "tile nodes must be in [0, 2816]");
+        g_tile_nodes = nodes;
+    });
+}
+
+int mpm_lame(double E, double nu, double* lam, double* mu)
+{
+    return guard([&] {
+        if (!lam || !mu) fail(MPM_ERR_ARG, "null output");
+        *lam = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        *mu = E / (2.0 + 2.0 * nu);
+    });
+}
+
+// ---------------------------------------------------------------- PointCloud
+
+int mpm_pointcloud_create(int n, int precision, mpm_pointcloud** out)
+{
+    return guard([&] {
+        if (!out || n < 0) fail(MPM_ERR_ARG, "bad arguments");
+        if (precision != MPM_FP32 && precision != MPM_FP64) fail(MPM_ERR_ARG, "bad precision %d", precision);
+        auto* pc = new mpm_pointcloud();
+        pc->d = new_pc(n, precision, nullptr);
+        ck(cudaStreamSynchronize(nullptr), "sync");
+        *out = pc;
+    });
+}
+
+int mpm_pointcloud_set(mpm_pointcloud* pc, int field, const void* src, int dtype, int on_device)
+{
+    return guard([&] {
+        check_pc(pc);
+        if (!src && pc->d->n) fail(MPM_ERR_ARG, "null source");
+        with_prec(pc->d->prec, [&](auto r) {
+            using R = decltype(r);
+            pc_set<R>(*pc->d, field, src, dtype, on_device, pc->stream);
+        });
+        ck(cudaStreamSynchronize(pc->stream), "sync");
+    });
+}
+
+int mpm_pointcloud_get(const mpm_pointcloud* pc, int field, void* dst, int dtype, int on_device)
+{
+    return guard([&] {
+        check_pc(pc);
+        if (!dst && pc->d->n) fail(MPM_ERR_ARG, "null destination");
+        with_prec(pc->d->prec, [&](auto r) {
+            using R = decltype(r);
+            pc_get<R>(*pc->d, field, dst, dtype, on_device, pc->stream);
+        });
+        ck(cudaStreamSynchronize(pc->stream), "sync");
+    });
+}
+
+int mpm_pointcloud_size(const mpm_pointcloud* pc, int* n)
+{
+    return guard([&] {
+        check_pc(pc);
+        *n = pc->d->n;
+    });
+}
+
+int mpm_pointcloud_precision(const mpm_pointcloud* pc, int* p)
+{
+    return guard([&] {
+        check_pc(pc);
+        *p = pc->d->prec;
+    });
+}
+
+int mpm_pointcloud_release(mpm_pointcloud* pc)
+{
+    delete pc;
+    return MPM_OK;
+}
+
+// ---------------------------------------------------------------------- Grid
+
+int mpm_grid_create(int nx, int ny, int nz, double dx, const double* min_point, int precision, mpm_grid** out)
+{
+    return guard([&] {
+        if (!out || nx <= 0 || ny <= 0 || nz <= 0 || !(dx > 0)) fail(MPM_ERR_ARG, "bad grid arguments");
+        if (precision != MPM_FP32 && precision != MPM_FP64) fail(MPM_ERR_ARG, "bad precision %d", precision);
+        auto g = std::make_shared<GridData>();
+        g->dims[0] = nx;
+        g->dims[1] = ny;
+        g->dims[2] = nz;
+        g->dx = dx;
+        for (int a = 0; a < 3; ++a) g->gmin[a] = min_point ? min_point[a] : 0.0;
+        g->prec = precision;
+        g->nodes = make_buf(esize(precision) * 4 * g->nn(), nullptr, true);
+        ck(cudaStreamSynchronize(nullptr), "sync");
+        auto* h = new mpm_grid();
+        h->d = g;
+        *out = h;
+    });
+}
+
+int mpm_grid_info(const mpm_grid* g, int* dims, double* dx, double* min_point)
+{
+    return guard([&] {
+        check_grid(g);
+        for (int a = 0; a < 3; ++a) {
+            if (dims) dims[a] = g->d->dims[a];
+            if (min_point) min_point[a] = g->d->gmin[a];
+        }
+        if (dx) *dx = g->d->dx;
+    });
+}
+
+int mpm_grid_get(const mpm_grid* g, int field, void* dst, int dtype, int on_device)
+{
+    return guard([&] {
+        check_grid(g);
+        if (field < 0 || field > 2) fail(MPM_ERR_ARG, "bad grid field %d", field);
+        with_prec(g->d->prec, [&](auto r) {
+            using R = decltype(r);
+            grid_get<R>(*g->d, field, dst, dtype, on_device, nullptr);
+        });
+    });
+}
+
+int mpm_grid_set(mpm_grid* g, int field, const void* src, int dtype, int on_device)
+{
+    return guard([&] {
+        check_grid(g);
+        if (field != MPM_GRID_MASS && field != MPM_GRID_MOMENTUM) fail(MPM_ERR_ARG, "bad grid field %d", field);
+        with_prec(g->d->prec, [&](auto r) {
+            using R = decltype(r);
+            grid_set<R>(*g->d, field, src, dtype, on_device, nullptr);
+        });
+    });
+}
+
+int mpm_grid_release(mpm_grid* g)
+{
+    delete g;
+    return MPM_OK;
+}
+
+int mpm_p2g(mpm_pointcloud* pc, mpm_grid* g)
+{
+    return guard([&] {
+        check_pc(pc);
+        check_grid(g);
+        if (pc->d->prec != g->d->prec) fail(MPM_ERR_ARG, "PointCloud and Grid precision differ");
+        StepCfg c = base_cfg(*g->d);
+        with_prec(pc->d->prec, [&](auto r) {
+            using R = decltype(r);
+            launch_p2g_plain<R>(c, pc->d->n, pc->d->ld, pc->d->st->as<R>(), pc->d->co->as<R>(), g->d->nodes->as<R>(),
+                                nullptr);
+        });
+        check_launch("p2g");
+        ck(cudaStreamSynchronize(nullptr), "sync");
+    });
+}
+
+int mpm_calculate_point_cloud_volumes(mpm_pointcloud* pc, mpm_grid* g)
+{
+    return guard([&] {
+        check_pc(pc);
+        check_grid(g);
+        if (pc->d->prec != g->d->prec) fail(MPM_ERR_ARG, "PointCloud and Grid precision differ");
+        StepCfg c = base_cfg(*g->d);
+        with_prec(pc->d->prec, [&](auto r) {
+            using R = decltype(r);
+            launch_p2g_plain<R>(c, pc->d->n, pc->d->ld, pc->d->st->as<R>(), pc->d->co->as<R>(), g->d->nodes->as<R>(),
+                                nullptr);
+            launch_volumes<R>(c, pc->d->n, pc->d->ld, pc->d->st->as<R>(), pc->d->co->as<R>(), g->d->nodes->as<R>(),
+                              nullptr);
+        });
+        check_launch("volumes");
+        ck(cudaStreamSynchronize(nullptr), "sync");
+    });
+}
+
+// ----------------------------------------------------------------- CompGraph
+
+int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_grid* target, const mpm_options* opt,
+                         mpm_compgraph** out)
+{
+    return guard([&] {
+        check_pc(pc);
+        check_grid(grid);
+        if (!out) fail(MPM_ERR_ARG, "null output");
+        std::unique_ptr<mpm_compgraph> cg(new mpm_compgraph());
+        Graph& G = cg->g;
+        mpm_default_options(&G.opt);
+        if (opt) G.opt = *opt;
+        if (G.opt.checkpoint_every < 1) G.opt.checkpoint_every = 1;
+        mpm_default_params(&G.prm);
+        G.prec = pc->d->prec;
+        if (G.opt.precision != G.prec) fail(MPM_ERR_ARG, "options.precision differs from the PointCloud's");
+        if (grid->d->prec != G.prec) fail(MPM_ERR_ARG, "grid precision differs from the PointCloud's");
+        ck(cudaStreamCreateWithFlags(&G.own, cudaStreamNonBlocking), "cudaStreamCreate");
+        G.stream = G.own;
+        G.geom.prec = grid->d->prec;
+        for (int a = 0; a < 3; ++a) {
+            G.geom.dims[a] = grid->d->dims[a];
+            G.geom.gmin[a] = grid->d->gmin[a];
+        }
+        G.geom.dx = grid->d->dx;
+        if (target) G.target = target->d;
+        ck(cudaStreamSynchronize(pc->stream), "sync");
+        G.base = clone_pc(*pc->d, G.stream, false);
+        G.base->grads.reset();
+        G.layers.resize(1);
+        G.layers[0].pc = G.base;
+        ck(cudaStreamSynchronize(G.stream), "sync");
+        *out = cg.release();
+    });
+}
+
+int mpm_compgraph_release(mpm_compgraph* cg)
+{
+    if (cg) cudaStreamSynchronize(cg->g.stream);
+    delete cg;
+    return MPM_OK;
+}
+
+int mpm_compgraph_set_params(mpm_compgraph* cg, const mpm_params* p)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (!p) fail(MPM_ERR_ARG, "null params");
+        cg->g.prm = *p;
+    });
+}
+
+int mpm_compgraph_get_params(const mpm_compgraph* cg, mpm_params* p)
+{
+    return guard([&] {
+        check_cg(cg);
+        *p = cg->g.prm;
+    });
+}
+
+int mpm_compgraph_get_options(const mpm_compgraph* cg, mpm_options* o)
+{
+    return guard([&] {
+        check_cg(cg);
+        *o = cg->g.opt;
+    });
+}
+
+int mpm_compgraph_set_stream(mpm_compgraph* cg, void* stream)
+{
+    return guard([&] {
+        check_cg(cg);
+        ck(cudaStreamSynchronize(cg->g.stream), "sync");
+        cg->g.stream = stream ? (cudaStream_t)stream : cg->g.own;
+    });
+}
+
+int mpm_compgraph_set_up(mpm_compgraph* cg, int num_layers)
+{
+    return guard([&] {
+        check_cg(cg);
+        with_prec(cg->g.prec, [&](auto r) { graph_set_up<decltype(r)>(cg->g, num_layers); });
+        ck(cudaStreamSynchronize(cg->g.stream), "sync");
+    });
+}
+
+int mpm_compgraph_num_layers(const mpm_compgraph* cg, int* out)
+{
+    return guard([&] {
+        check_cg(cg);
+        *out = (int)cg->g.layers.size();
+    });
+}
+
+int mpm_compgraph_forward(mpm_compgraph* cg, int start_layer, int episode)
+{
+    (void)episode;
+    return guard([&] {
+        check_cg(cg);
+        with_prec(cg->g.prec, [&](auto r) { graph_forward<decltype(r)>(cg->g, start_layer); });
+        ck(cudaStreamSynchronize(cg->g.stream), "forward");
+    });
+}
+
+int mpm_compgraph_backward(mpm_compgraph* cg, int control_layer)
+{
+    return guard([&] {
+        check_cg(cg);
+        with_prec(cg->g.prec, [&](auto r) { graph_backward<decltype(r)>(cg->g, control_layer); });
+        ck(cudaStreamSynchronize(cg->g.stream), "backward");
+    });
+}
+
+int mpm_compgraph_mass_loss(mpm_compgraph* cg, double* loss)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (!loss) fail(MPM_ERR_ARG, "null output");
+        with_prec(cg->g.prec, [&](auto r) { *loss = graph_loss<decltype(r)>(cg->g); });
+    });
+}
+
+int mpm_compgraph_accumulate_render_grads(mpm_compgraph* cg, const float* dLdF, const float* dLdx, int n)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (G.layers.empty()) fail(MPM_ERR_STATE, "CompGraph has no layers!");
+        PCData& last = *G.layers.back().pc;
+        if (n != last.n)
+            fail(MPM_ERR_SHAPE, "Shape mismatch: point cloud has %d points, but got dLdF with %d and dLdx with %d",
+                 last.n, n, n);
+        with_prec(G.prec, [&](auto r) {
+            using R = decltype(r);
+            cudaStream_t s = G.stream;
+            ensure_grads(last, s);
+            DevBuf tmp((size_t)12 * last.ld * sizeof(R));
+            planes_in<R>(n, 9, last.ld, dLdF, MPM_DTYPE_F32, 0, tmp.as<R>(), s);
+            planes_in<R>(n, 3, last.ld, dLdx, MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s);
+            launch_axpy_planes<R>(n, 9, last.ld, R(1), tmp.as<R>(), last.grads->as<R>() + ST_F * last.ld, s);
+            launch_axpy_planes<R>(n, 3, last.ld, R(1), tmp.as<R>() + 9 * last.ld, last.grads->as<R>() + ST_X * last.ld,
+                                  s);
+            check_launch("accumulate");
+            ck(cudaStreamSynchronize(s), "sync");
+        });
+    });
+}
+
+int mpm_compgraph_set_render_gradients(mpm_compgraph* cg, const float* dLdF, const float* dLdx, int n)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (G.layers.empty()) fail(MPM_ERR_STATE, "CompGraph has no layers!");
+        if (n < 0) fail(MPM_ERR_SHAPE, "bad point count");
+        G.rgF.assign(dLdF, dLdF + (size_t)n * 9);
+        G.rgx.assign(dLdx, dLdx + (size_t)n * 3);
+        G.has_rg = true;
+        G.rg_n = (size_t)n;
+        double nf = 0, nx = 0;
+        for (float v : G.rgF) nf += (double)v * v;
+        for (float v : G.rgx) nx += (double)v * v;
+        say("[C++] Stored render gradients for %d points\n", n);
+        say("[C++]   ||dL_render/dF|| = %g\n", std::sqrt(nf));
+        say("[C++]   ||dL_render/dx|| = %g\n", std::sqrt(nx));
+    });
+}
+
+int mpm_compgraph_clear_render_gradients(mpm_compgraph* cg)
+{
+    return guard([&] {
+        check_cg(cg);
+        cg->g.rgF.clear();
+        cg->g.rgx.clear();
+        cg->g.has_rg = false;
+        cg->g.rg_n = 0;
+        say("[C++] Cleared render gradients\n");
+    });
+}
+
+int mpm_compgraph_render_gradient_info(const mpm_compgraph* cg, int* has, int* num_points, double* nF, double* nx)
+{
+    return guard([&] {
+        check_cg(cg);
+        const Graph& G = cg->g;
+        double f = 0, x = 0;
+        if (G.has_rg) {
+            for (float v : G.rgF) f += (double)v * v;
+            for (float v : G.rgx) x += (double)v * v;
+        }
+        if (has) *has = G.has_rg;
+        if (num_points) *num_points = (int)G.rg_n;
+        if (nF) *nF = std::sqrt(f);
+        if (nx) *nx = std::sqrt(x);
+    });
+}
+
+int mpm_compgraph_layer(mpm_compgraph* cg, int layer, mpm_pointcloud** out)
+{
+    return guard([&] {
+        check_cg(cg);
+        const int L = (int)cg->g.layers.size();
+        if (layer < 0 || layer >= L) fail(MPM_ERR_RANGE, "Timestep index %d out of range [0, %d)", layer, L);
+        if (!out) fail(MPM_ERR_ARG, "null output");
+        auto* pc = new mpm_pointcloud();
+        pc->d = cg->g.layers[layer].pc;
+        pc->stream = cg->g.stream;
+        ck(cudaStreamSynchronize(cg->g.stream), "sync");
+        *out = pc;
+    });
+}
+
+int mpm_compgraph_promote_last_as_initial(mpm_compgraph* cg, int carry_grid)
+{
+    (void)carry_grid;  // grids are reset at the start of every step
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (G.layers.empty()) return;
+        if (!G.layers.back().pc->have_state) fail(MPM_ERR_STATE, "last layer not stored");
+        G.layers.front().pc = G.layers.back().pc;
+        G.layers.resize(1);
+        G.base = G.layers[0].pc;
+    });
+}
+
+int mpm_compgraph_grad_norm(mpm_compgraph* cg, int layer, double* out)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (layer < 0 || layer >= (int)cg->g.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
+        with_prec(cg->g.prec, [&](auto r) { *out = graph_grad_norm<decltype(r)>(cg->g, layer); });
+    });
+}
+
+int mpm_compgraph_adam_step(mpm_compgraph* cg, int layer, double alpha, double gnorm, double b1, double b2, double eps,
+                            int timestep)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (layer < 0 || layer >= (int)cg->g.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
+        with_prec(cg->g.prec, [&](auto r) { graph_adam<decltype(r)>(cg->g, layer, alpha, gnorm, b1, b2, eps, timestep); });
+        ck(cudaStreamSynchronize(cg->g.stream), "adam");
+    });
+}
+
+int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int t, int max_gd, int episode, double alpha,
+                                           int max_ls)
+{
+    return guard([&] {
+        check_cg(cg);
+        with_prec(cg->g.prec, [&](auto r) { graph_optimize_single<decltype(r)>(cg->g, t, max_gd, episode, alpha, max_ls); });
+        ck(cudaStreamSynchronize(cg->g.stream), "optimize");
+    });
+}
+
+int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (!opt) fail(MPM_ERR_ARG, "null OptInput");
+        if (opt->num_timesteps < 1) fail(MPM_ERR_ARG, "num_timesteps must be positive");
+        with_prec(cg->g.prec, [&](auto r) { graph_run_optimization<decltype(r)>(cg->g, *opt); });
+        ck(cudaStreamSynchronize(cg->g.stream), "run_optimization");
+    });
+}
+
+int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long* out)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (layer < 0 || layer >= (int)G.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
+        const Buf& gb = G.layers[layer].grid ? G.layers[layer].grid : G.fgrid;
+        if (!gb) fail(MPM_ERR_STATE, "layer %d has no forward grid", layer);
+        DevBuf d(sizeof(unsigned long long));
+        StepCfg c = G.cfg();
+        with_prec(G.prec, [&](auto r) {
+            using R = decltype(r);
+            launch_count_active<R>(c, gb->as<R>(), d.as<unsigned long long>(), G.stream);
+        });
+        check_launch("count_active");
+        ck(cudaMemcpyAsync(out, d.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, G.stream), "D2H");
+        ck(cudaStreamSynchronize(G.stream), "sync");
+    });
+}
+
+int mpm_profile_enable(int on)
+{
+    return guard([&] {
+        g_prof.resolve();
+        g_prof.on = on != 0;
+    });
+}
+
+int mpm_profile_reset(void)
+{
+    return guard([&] {
+        g_prof.resolve();
+        for (int i = 0; i < K_COUNT; ++i) {
+            g_prof.count[i] = 0;
+            g_prof.ms[i] = 0;
+        }
+    });
+}
+
+int mpm_profile_query(int kernel, long long* launches, double* total_ms)
+{
+    return guard([&] {
+        if (kernel < 0 || kernel >= K_COUNT) fail(MPM_ERR_RANGE, "kernel id %d out of range", kernel);
+        g_prof.resolve();
+        if (launches) *launches = g_prof.count[kernel];
+        if (total_ms) *total_ms = g_prof.ms[kernel];
+    });
+}
+
+const char* mpm_kernel_name(int kernel) { return (kernel >= 0 && kernel < K_COUNT) ? k_names[kernel] : ""; }
+
+long long mpm_launch_count(void) { return g_prof.launches; }
+
+int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on)
+{
+    return guard([&] {
+        check_cg(cg);
+        cg->g.lame_on = on != 0;
+    });
+}
+
+int mpm_compgraph_synchronize(mpm_compgraph* cg)
+{
+    return guard([&] {
+        check_cg(cg);
+        ck(cudaStreamSynchronize(cg->g.stream), "sync");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,1219 @@
+// mpm_kernels.cu -- sm_103a kernels for the differentiable MPM step.
+//
+// Forward step (DiffMPMLib3D/ForwardSimulation.cpp:159-185) as three kernels:
+//   k_p2g         P_op_1 + P2G: FCR stress fused into the momentum scatter,
+//                 accumulated in a shared-memory node tile, flushed with few
+//                 global atomics (ForwardSimulation.cpp:16-80)
+//   k_grid_update mass clamp + G_op (ForwardSimulation.cpp:82-87,165-170)
+//   k_g2p         G2P + P_op_2: velocity/affine gather, trust region,
+//                 F update, smoothing, advection (ForwardSimulation.cpp:89-157)
+// Adjoint step (DiffMPMLib3D/BackPropagation.cpp:9-144) as three kernels:
+//   k_g2p_adj     P_op_2^T + G2P^T scatter of dL/dv_next, dL/dC_next
+//   k_grid_adj    G_op^T per node
+//   k_p2g_adj     P2G^T gather + stress VJP (P_op_1^T), matrix-free
+// No kernel here uses tensor cores: nothing on this path is a dense
+// contraction; the bound is memory traffic and FP32 issue rate.
+#include <algorithm>
+#include <climits>
+#include <cstdint>
+
+#include "mpm_launch.h"
+#include "mpm_math.cuh"
+
+namespace mpm {
+
+int g_tile_nodes = 2048;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename R>
+struct KP {
+    R dt, dragf, s, bulk, jmin, C0, dx, inv_dx;
+    R gmin[3], dtf[3];
+    int dims[3];
+    int material, exact;
+};
+
+template <typename R>
+KP<R> make_kp(const StepCfg& c)
+{
+    KP<R> k;
+    k.dt = (R)c.dt;
+    k.dragf = (R)(1.0 - c.dt * c.drag);
+    k.s = (R)c.smoothing;
+    k.bulk = (R)c.bulk;
+    k.jmin = (R)c.jmin;
+    k.C0 = (R)((c.kernel == 0 ? 3.0 : 4.0) / (c.dx * c.dx));
+    k.dx = (R)c.dx;
+    k.inv_dx = (R)(1.0 / c.dx);
+    for (int a = 0; a < 3; ++a) {
+        k.gmin[a] = (R)c.gmin[a];
+        k.dtf[a] = (R)(c.dt * c.fext[a]);
+        k.dims[a] = c.dims[a];
+    }
+    k.material = c.material;
+    k.exact = c.exact;
+    return k;
+}
+
+inline int nblocks(long long n, int t = kThreads) { return (int)((n + t - 1) / t); }
+
+// select a[i] from a small register array without dynamic indexing
+template <typename R, int K>
+MPM_D R sel(const R (&a)[K], int i)
+{
+    R r = a[0];
+#pragma unroll
+    for (int q = 1; q < K; ++q) r = (i == q) ? a[q] : r;
+    return r;
+}
+
+template <typename R>
+MPM_D void load_planes(const R* __restrict__ base, long long ld, int p, int k, R* out)
+{
+#pragma unroll
+    for (int i = 0; i < k; ++i) out[i] = base[(long long)i * ld + p];
+}
+
+template <typename R>
+MPM_D void store_planes(R* __restrict__ base, long long ld, int p, int k, const R* v)
+{
+#pragma unroll
+    for (int i = 0; i < k; ++i) base[(long long)i * ld + p] = v[i];
+}
+
+template <typename R>
+MPM_D bool in_grid(const KP<R>& kp, int i, int j, int k)
+{
+    return (unsigned)i < (unsigned)kp.dims[0] && (unsigned)j < (unsigned)kp.dims[1] && (unsigned)k < (unsigned)kp.dims[2];
+}
+
+template <typename R>
+MPM_D long long node_of(const KP<R>& kp, int i, int j, int k)
+{
+    return ((long long)i * kp.dims[1] + j) * kp.dims[2] + k;
+}
+
+// Ft = F + dFc
+template <typename R>
+MPM_D void load_Ft(const R* st, const R* dfc, long long ld, int p, R* F, R* Ft)
+{
+    load_planes(st + ST_F * ld, ld, p, 9, F);
+    if (dfc) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ft[i] = F[i] + dfc[(long long)i * ld + p];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ft[i] = F[i];
+    }
+}
+
+// ------------------------------------------------------------------------
+// Scatter machinery shared by P2G (4 components: p0,p1,p2,m) and the G2P
+// transpose (3 components: dL/dv).  A block owns a contiguous chunk of
+// particles; when the chunk's stencil bounding box fits the shared tile
+// budget, contributions are accumulated with shared-memory atomics and
+// flushed once, otherwise they go straight to global atomics.  Each lane
+// starts its walk over the stencil at a different (b,c) so lanes of one cell
+// rarely hit the same node in the same instruction.
+// ------------------------------------------------------------------------
+
+template <typename R, int K, int NC>
+struct Scatter {
+    int b0, b1, b2, e0, e1, e2;
+    bool tile;
+    R* sm;
+    int vol;
+
+    MPM_D void setup(bool valid, const int* base, void* smem, int tile_cap)
+    {
+        __shared__ int box[6];
+        if (threadIdx.x < 3) box[threadIdx.x] = INT_MAX;
+        else if (threadIdx.x < 6) box[threadIdx.x] = INT_MIN;
+        __syncthreads();
+        tile = false;
+        if (tile_cap > 0) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                int lo = valid ? base[a] : INT_MAX;
+                int hi = valid ? base[a] : INT_MIN;
+                lo = __reduce_min_sync(0xffffffffu, lo);
+                hi = __reduce_max_sync(0xffffffffu, hi);
+                if ((threadIdx.x & 31) == 0) {
+                    atomicMin(&box[a], lo);
+                    atomicMax(&box[3 + a], hi);
+                }
+            }
+        }
+        __syncthreads();
+        if (tile_cap > 0 && box[0] != INT_MAX) {
+            b0 = box[0];
+            b1 = box[1];
+            b2 = box[2];
+            long long x0 = (long long)box[3] - box[0] + K, x1 = (long long)box[4] - box[1] + K,
+                      x2 = (long long)box[5] - box[2] + K;
+            long long v = x0 * x1 * x2;
+            if (v <= tile_cap) {
+                tile = true;
+                e0 = (int)x0;
+                e1 = (int)x1;
+                e2 = (int)x2;
+                vol = (int)v;
+                sm = reinterpret_cast<R*>(smem);
+                for (int t = threadIdx.x; t < NC * vol; t += blockDim.x) sm[t] = R(0);
+            }
+        }
+        __syncthreads();
+    }
+
+    MPM_D void add(const KP<R>& kp, R* __restrict__ grid, int i, int j, int k, const R* val)
+    {
+        if (tile) {
+            int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
+#pragma unroll
+            for (int q = 0; q < NC; ++q) atomicAdd(&sm[q * vol + idx], val[q]);
+        } else if (in_grid(kp, i, j, k)) {
+            long long nd = node_of(kp, i, j, k);
+#pragma unroll
+            for (int q = 0; q < NC; ++q) atomicAdd(&grid[nd * 4 + q], val[q]);
+        }
+    }
+
+    MPM_D void flush(const KP<R>& kp, R* __restrict__ grid)
+    {
+        __syncthreads();
+        if (!tile) return;
+        for (int t = threadIdx.x; t < vol; t += blockDim.x) {
+            R v[NC];
+            bool any = false;
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                v[q] = sm[q * vol + t];
+                any |= (v[q] != R(0));
+            }
+            if (!any) continue;
+            int kk = t % e2, r = t / e2;
+            int jj = r % e1, ii = r / e1;
+            int i = b0 + ii, j = b1 + jj, k = b2 + kk;
+            if (!in_grid(kp, i, j, k)) continue;
+            long long nd = node_of(kp, i, j, k);
+#pragma unroll
+            for (int q = 0; q < NC; ++q)
+                if (v[q] != R(0)) atomicAdd(&grid[nd * 4 + q], v[q]);
+        }
+    }
+};
+
+// Walk the K^3 stencil, calling f(i, j, k, w, dg) with a lane-dependent order.
+template <typename R, int K, typename Fn>
+MPM_D void walk_rotated(const Stencil<R, K>& st, Fn&& f)
+{
+    const int lane = threadIdx.x & 31;
+    const int rb = (lane >> 2) % K, rc = lane % K;
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        const R wa = st.w[0][a], ga = st.g[0][a];
+#pragma unroll
+        for (int bb = 0; bb < K; ++bb) {
+            int b = bb + rb;
+            b = b >= K ? b - K : b;
+            const R wab = wa * sel(st.w[1], b), gb = sel(st.g[1], b);
+#pragma unroll
+            for (int cc = 0; cc < K; ++cc) {
+                int c = cc + rc;
+                c = c >= K ? c - K : c;
+                const R w = wab * sel(st.w[2], c), gc = sel(st.g[2], c);
+                f(st.base[0] + a, st.base[1] + b, st.base[2] + c, w, ga, gb, gc);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ P2G
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_p2g(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                   const R* __restrict__ dfc, const R* __restrict__ co,
+                                                   R* __restrict__ grid, int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    Stencil<R, K> sten;
+    R A[9], mv[3], mass = R(0);
+    if (valid) {
+        R x[3], v[3], C[9], F[9], Ft[9];
+        load_planes(st + ST_X * ld, ld, p, 3, x);
+        load_planes(st + ST_V * ld, ld, p, 3, v);
+        load_planes(st + ST_C * ld, ld, p, 9, C);
+        load_Ft(st, dfc, ld, p, F, Ft);
+        mass = co[CO_M * ld + p];
+        const R vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
+        Inv<R> iv;
+        invariants(Ft, iv);
+        R P[9], Rm[9], S[9], PF[9];
+        pk(kp.material, Ft, lam, mu, iv, P, Rm, S);
+        mulNT3(P, Ft, PF);
+        const R trC = C[0] + C[4] + C[8];
+        const R k1 = -kp.C0 * kp.dt * vol;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = k1 * (PF[i] + ((i % 4 == 0) ? kp.bulk * trC : R(0))) + mass * C[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) mv[a] = mass * v[a] * kp.dragf;
+        make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    Scatter<R, K, 4> sc;
+    sc.setup(valid, sten.base, smem, tile_cap);
+    if (valid) {
+        walk_rotated<R, K>(sten, [&](int i, int j, int k, R w, R gx, R gy, R gz) {
+            R val[4];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) val[r] = w * (mv[r] + A[r * 3] * gx + A[r * 3 + 1] * gy + A[r * 3 + 2] * gz);
+            val[3] = w * mass;
+            sc.add(kp, grid, i, j, k, val);
+        });
+    }
+    sc.flush(kp, grid);
+}
+
+// -------------------------------------------------------- grid update
+
+template <typename R>
+__global__ void k_grid_update(KP<R> kp, long long nn, R* __restrict__ grid)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    R* g = grid + 4 * i;
+    R m = g[3];
+    if (m < R(0)) m = R(0);
+    R v0 = 0, v1 = 0, v2 = 0;
+    if (m > R(1e-12)) {
+        v0 = g[0] / m + kp.dtf[0];
+        v1 = g[1] / m + kp.dtf[1];
+        v2 = g[2] / m + kp.dtf[2];
+    }
+    g[0] = v0;
+    g[1] = v1;
+    g[2] = v2;
+    g[3] = m;
+}
+
+// load the 3 velocity components of node nd
+template <typename R>
+MPM_D void load_node3(const R* __restrict__ grid, long long nd, R* v);
+template <>
+MPM_D void load_node3<float>(const float* __restrict__ grid, long long nd, float* v)
+{
+    float4 q = __ldg(reinterpret_cast<const float4*>(grid) + nd);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+}
+template <>
+MPM_D void load_node3<double>(const double* __restrict__ grid, long long nd, double* v)
+{
+    double2 a = __ldg(reinterpret_cast<const double2*>(grid) + 2 * nd);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = __ldg(grid + 4 * nd + 2);
+}
+template <typename R>
+MPM_D void load_node4(const R* __restrict__ grid, long long nd, R* v);
+template <>
+MPM_D void load_node4<float>(const float* __restrict__ grid, long long nd, float* v)
+{
+    float4 q = __ldg(reinterpret_cast<const float4*>(grid) + nd);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+template <>
+MPM_D void load_node4<double>(const double* __restrict__ grid, long long nd, double* v)
+{
+    double2 a = __ldg(reinterpret_cast<const double2*>(grid) + 2 * nd);
+    double2 b = __ldg(reinterpret_cast<const double2*>(grid) + 2 * nd + 1);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+
+// ------------------------------------------------------------------ G2P
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                   const R* __restrict__ dfc, const R* __restrict__ grid,
+                                                   R* __restrict__ st1, R* __restrict__ trust)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3], F[9], Ft[9];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    load_Ft(st, dfc, ld, p, F, Ft);
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    // separable accumulation: v = sum w v_i, Cacc[:,a] = sum w v_i dg_a
+    R vs[3] = {0, 0, 0}, Cx[3] = {0, 0, 0}, Cy[3] = {0, 0, 0}, Cz[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        const int i = sn.base[0] + a;
+        if ((unsigned)i >= (unsigned)kp.dims[0]) continue;
+        R t0[3] = {0, 0, 0}, t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+#pragma unroll
+        for (int b = 0; b < K; ++b) {
+            const int j = sn.base[1] + b;
+            if ((unsigned)j >= (unsigned)kp.dims[1]) continue;
+            R s0[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+            const long long row = ((long long)i * kp.dims[1] + j) * kp.dims[2];
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                const int k = sn.base[2] + c;
+                if ((unsigned)k >= (unsigned)kp.dims[2]) continue;
+                R vi[3];
+                load_node3(grid, row + k, vi);
+                const R wz = sn.w[2][c], wzg = wz * sn.g[2][c];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    s0[r] += wz * vi[r];
+                    s2[r] += wzg * vi[r];
+                }
+            }
+            const R wy = sn.w[1][b], wyg = wy * sn.g[1][b];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                t0[r] += wy * s0[r];
+                t1[r] += wyg * s0[r];
+                t2[r] += wy * s2[r];
+            }
+        }
+        const R wx = sn.w[0][a], wxg = wx * sn.g[0][a];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            vs[r] += wx * t0[r];
+            Cx[r] += wxg * t0[r];
+            Cy[r] += wx * t1[r];
+            Cz[r] += wx * t2[r];
+        }
+    }
+    R Cn[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        Cn[r * 3 + 0] = kp.C0 * Cx[r];
+        Cn[r * 3 + 1] = kp.C0 * Cy[r];
+        Cn[r * 3 + 2] = kp.C0 * Cz[r];
+    }
+    // J trust region (ForwardSimulation.cpp:135-152)
+    R s_tr = R(1);
+    if (kp.jmin > R(0)) {
+        R J0 = R(1) + det_minus_one(Ft);
+        J0 = J0 > R(1e-6) ? J0 : R(1e-6);
+        const R trC = Cn[0] + Cn[4] + Cn[8];
+        if (trC < R(0)) {
+            const R denom = kp.dt * trC;
+            const R s = (kp.jmin / J0 - R(1)) / (denom < R(-1e-6) ? denom : R(-1e-6));
+            if (s < R(1)) {
+                s_tr = s < R(0) ? R(0) : s;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Cn[i] *= s_tr;
+            }
+        }
+    }
+    R IdtC[9], Fn[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IdtC[i] = ((i % 4 == 0) ? R(1) : R(0)) + kp.dt * Cn[i];
+    mul3(IdtC, Ft, Fn);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fn[i] = Fn[i] * (R(1) - kp.s) + F[i] * kp.s;
+    R x1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x1[a] = x[a] + kp.dt * vs[a];
+    store_planes(st1 + ST_X * ld, ld, p, 3, x1);
+    store_planes(st1 + ST_V * ld, ld, p, 3, vs);
+    store_planes(st1 + ST_C * ld, ld, p, 9, Cn);
+    store_planes(st1 + ST_F * ld, ld, p, 9, Fn);
+    if (trust) trust[p] = s_tr;
+}
+
+// ------------------------------------------------------------- adjoint
+
+// P_op_2^T for one particle (BackPropagation.cpp:22-32): dL/dv_next, dL/dC_next
+// and the part of dL/dFt that does not pass through the grid.  In exact mode
+// the trust-region scale of the step is differentiated as well.
+template <typename R>
+struct PostAdj {
+    R vbar[3], Cbar[9], Fpart[9];
+};
+
+template <typename R>
+MPM_D void post_adjoint(const KP<R>& kp, long long ld, int p, const R* Ft, const R* __restrict__ st1,
+                        const R* __restrict__ g1, const R* __restrict__ trust, PostAdj<R>& o)
+{
+    R C1[9], gF1[9], gx1[3], gv1[3], gC1[9];
+    load_planes(st1 + ST_C * ld, ld, p, 9, C1);
+    load_planes(g1 + ST_F * ld, ld, p, 9, gF1);
+    load_planes(g1 + ST_X * ld, ld, p, 3, gx1);
+    load_planes(g1 + ST_V * ld, ld, p, 3, gv1);
+    load_planes(g1 + ST_C * ld, ld, p, 9, gC1);
+    R IdtC[9], t[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IdtC[i] = ((i % 4 == 0) ? R(1) : R(0)) + kp.dt * C1[i];
+    mulTN3(IdtC, gF1, t);  // (I + dt C1)^T g
+#pragma unroll
+    for (int a = 0; a < 3; ++a) o.vbar[a] = kp.dt * gx1[a] + gv1[a];
+    R gFtT[9];
+    mulNT3(gF1, Ft, gFtT);  // g Ft^T
+    const R cf = kp.exact ? (R(1) - kp.s) * kp.dt : kp.dt;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) o.Cbar[i] = cf * gFtT[i] + gC1[i];
+    if (kp.exact) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o.Fpart[i] = (R(1) - kp.s) * t[i];
+        if (kp.jmin > R(0) && trust) {
+            const R s_tr = trust[p];
+            if (s_tr <= R(0)) {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) o.Cbar[i] = R(0);
+            } else if (s_tr < R(1)) {
+                R Cp[9];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Cp[i] = C1[i] / s_tr;
+                const R trCp = Cp[0] + Cp[4] + Cp[8];
+                const R denom = kp.dt * trCp;
+                const R q = dot9(o.Cbar, Cp);
+                const R dsdtr = denom < R(-1e-6) ? -s_tr / trCp : R(0);
+                R c[9];
+                cof3(Ft, c);
+                const R J0 = R(1) + det_minus_one(Ft);
+                const R dsdJ0 = J0 > R(1e-6) ? -kp.jmin / (J0 * J0 * (denom < R(-1e-6) ? denom : R(-1e-6))) : R(0);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) {
+                    o.Cbar[i] = s_tr * o.Cbar[i] + ((i % 4 == 0) ? q * dsdtr : R(0));
+                    o.Fpart[i] += q * dsdJ0 * c[i];  // J0 Ft^{-T} = cof(Ft)
+                }
+            }
+        }
+    } else {
+        // reference: (1-s)(I+dtC1)^T g + s g, plus the second (I+dtC1)^T g
+        // that BackPropagation.cpp:140 adds
+#pragma unroll
+        for (int i = 0; i < 9; ++i) o.Fpart[i] = (R(2) - kp.s) * t[i] + kp.s * gF1[i];
+    }
+}
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_g2p_adj(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                       const R* __restrict__ dfc, const R* __restrict__ st1,
+                                                       const R* __restrict__ g1, const R* __restrict__ trust,
+                                                       R* __restrict__ adj, int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    Stencil<R, K> sten;
+    R vb[3], CC[9];
+    if (valid) {
+        R x[3], F[9], Ft[9];
+        load_planes(st + ST_X * ld, ld, p, 3, x);
+        load_Ft(st, dfc, ld, p, F, Ft);
+        PostAdj<R> o;
+        post_adjoint(kp, ld, p, Ft, st1, g1, trust, o);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) vb[a] = o.vbar[a];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) CC[i] = kp.C0 * o.Cbar[i];
+        make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    Scatter<R, K, 3> sc;
+    sc.setup(valid, sten.base, smem, tile_cap);
+    if (valid) {
+        walk_rotated<R, K>(sten, [&](int i, int j, int k, R w, R gx, R gy, R gz) {
+            R val[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) val[r] = w * (vb[r] + CC[r * 3] * gx + CC[r * 3 + 1] * gy + CC[r * 3 + 2] * gz);
+            sc.add(kp, adj, i, j, k, val);
+        });
+    }
+    sc.flush(kp, adj);
+}
+
+// G_op^T (BackPropagation.cpp:59-72)
+template <typename R>
+__global__ void k_grid_adj(KP<R> kp, long long nn, const R* __restrict__ grid, R* __restrict__ adj)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const R* g = grid + 4 * i;
+    R* d = adj + 4 * i;
+    const R m = g[3];
+    if (fabs(m) > R(1e-12)) {
+        R v0 = g[0], v1 = g[1], v2 = g[2];
+        if (kp.exact) {
+            v0 -= kp.dtf[0];
+            v1 -= kp.dtf[1];
+            v2 -= kp.dtf[2];
+        }
+        const R d0 = d[0], d1 = d[1], d2 = d[2];
+        const R im = R(1) / m;
+        d[3] = -(v0 * d0 + v1 * d1 + v2 * d2) * im;
+        d[0] = d0 * im;
+        d[1] = d1 * im;
+        d[2] = d2 * im;
+    } else {
+        d[0] = d[1] = d[2] = d[3] = R(0);
+    }
+}
+
+// P2G^T + P_op_1^T (BackPropagation.cpp:76-143)
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_p2g_adj(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                       const R* __restrict__ dfc, const R* __restrict__ co,
+                                                       const R* __restrict__ st1, const R* __restrict__ g1,
+                                                       const R* __restrict__ trust, const R* __restrict__ grid,
+                                                       const R* __restrict__ adj, R* __restrict__ g,
+                                                       R* __restrict__ gFt_out, R* __restrict__ glam,
+                                                       R* __restrict__ gmu)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3], v[3], C[9], F[9], Ft[9];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    load_planes(st + ST_V * ld, ld, p, 3, v);
+    load_planes(st + ST_C * ld, ld, p, 9, C);
+    load_Ft(st, dfc, ld, p, F, Ft);
+    const R mass = co[CO_M * ld + p], vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
+    Inv<R> iv;
+    invariants(Ft, iv);
+    R P[9], Rm[9], S[9], PF[9], A[9];
+    pk(kp.material, Ft, lam, mu, iv, P, Rm, S);
+    mulNT3(P, Ft, PF);
+    const R trC = C[0] + C[4] + C[8];
+    const R k1 = -kp.C0 * kp.dt * vol;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = k1 * (PF[i] + ((i % 4 == 0) ? kp.bulk * trC : R(0))) + mass * C[i];
+    R mvv[3];
+    const R mf = kp.exact ? kp.dragf : R(1);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) mvv[a] = mass * v[a] * mf;
+    PostAdj<R> o;
+    post_adjoint(kp, ld, p, Ft, st1, g1, trust, o);
+    R CC[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) CC[i] = kp.C0 * o.Cbar[i];
+
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, true);
+    R M1[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ax[3] = {0, 0, 0}, bp[3] = {0, 0, 0}, bv[3] = {0, 0, 0};
+    const R nidx = -kp.inv_dx;
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        const int i = sn.base[0] + a;
+        if ((unsigned)i >= (unsigned)kp.dims[0]) continue;
+#pragma unroll
+        for (int b = 0; b < K; ++b) {
+            const int j = sn.base[1] + b;
+            if ((unsigned)j >= (unsigned)kp.dims[1]) continue;
+            const long long row = ((long long)i * kp.dims[1] + j) * kp.dims[2];
+            const R wab = sn.w[0][a] * sn.w[1][b];
+            const R gwx_ab = nidx * sn.s[0][a] * sn.w[1][b], gwy_ab = nidx * sn.w[0][a] * sn.s[1][b];
+            const R dgx = sn.g[0][a], dgy = sn.g[1][b];
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                const int k = sn.base[2] + c;
+                if ((unsigned)k >= (unsigned)kp.dims[2]) continue;
+                R d[4], vi[3];
+                load_node4(adj, row + k, d);
+                load_node3(grid, row + k, vi);
+                const R w = wab * sn.w[2][c];
+                const R gw0 = gwx_ab * sn.w[2][c], gw1 = gwy_ab * sn.w[2][c], gw2 = nidx * wab * sn.s[2][c];
+                const R dgz = sn.g[2][c];
+                R Adg[3], cdg[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    Adg[r] = A[r * 3] * dgx + A[r * 3 + 1] * dgy + A[r * 3 + 2] * dgz;
+                    cdg[r] = CC[r * 3] * dgx + CC[r * 3 + 1] * dgy + CC[r * 3 + 2] * dgz;
+                }
+                const R sig = mass * d[3] + (mvv[0] + Adg[0]) * d[0] + (mvv[1] + Adg[1]) * d[1] +
+                              (mvv[2] + Adg[2]) * d[2] + vi[0] * (o.vbar[0] + cdg[0]) +
+                              vi[1] * (o.vbar[1] + cdg[1]) + vi[2] * (o.vbar[2] + cdg[2]);
+                ax[0] += sig * gw0;
+                ax[1] += sig * gw1;
+                ax[2] += sig * gw2;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const R wd = w * d[r];
+                    bp[r] += wd;
+                    bv[r] += w * vi[r];
+                    M1[r * 3 + 0] += wd * dgx;
+                    M1[r * 3 + 1] += wd * dgy;
+                    M1[r * 3 + 2] += wd * dgz;
+                }
+            }
+        }
+    }
+    R gx1[3];
+    load_planes(g1 + ST_X * ld, ld, p, 3, gx1);
+    R gx[3], gv[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const R AtB = A[r] * bp[0] + A[3 + r] * bp[1] + A[6 + r] * bp[2];
+        const R CtV = CC[r] * bv[0] + CC[3 + r] * bv[1] + CC[6 + r] * bv[2];
+        gx[r] = ax[r] - AtB - CtV + gx1[r];
+        gv[r] = mass * kp.dragf * bp[r];
+    }
+    R gC[9];
+    const R kb = k1 * kp.bulk;
+    const R trM = M1[0] + M1[4] + M1[8];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        R add = R(0);
+        if (i % 4 == 0) add = kp.exact ? kb * trM : kb * M1[i];
+        gC[i] = mass * M1[i] + add;
+    }
+    R t1[9], t2[9], gP[9], hv[9], gF[9];
+    mul3(M1, Ft, t1);
+    mulTN3(M1, P, t2);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gP[i] = k1 * t1[i];
+    pk_vjp(kp.material, kp.exact != 0, Ft, lam, mu, iv, Rm, S, gP, hv);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) gF[i] = o.Fpart[i] + k1 * t2[i] + hv[i];
+    if (gFt_out) store_planes(gFt_out, ld, p, 9, gF);
+    if (kp.exact) {
+        R gF1[9];
+        load_planes(g1 + ST_F * ld, ld, p, 9, gF1);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) gF[i] += kp.s * gF1[i];
+    }
+    store_planes(g + ST_X * ld, ld, p, 3, gx);
+    store_planes(g + ST_V * ld, ld, p, 3, gv);
+    store_planes(g + ST_F * ld, ld, p, 9, gF);
+    store_planes(g + ST_C * ld, ld, p, 9, gC);
+    if (glam || gmu) {
+        R dm = 0, dl = 0;
+        if (kp.material == MAT_FCR) {
+            const R kk = iv.Jm1c * iv.Jc;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                dm += gP[i] * R(2) * (Ft[i] - Rm[i]);
+                dl += gP[i] * kk * iv.Fit[i];
+            }
+        } else {
+            const R lj = log(iv.Jc);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                dm += gP[i] * (Ft[i] - iv.Fit[i]);
+                dl += gP[i] * lj * iv.Fit[i];
+            }
+        }
+        if (gmu) gmu[p] += dm;
+        if (glam) glam[p] += dl;
+    }
+}
+
+// ---------------------------------------------------------------- loss
+
+template <typename R>
+MPM_D double block_sum(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_mass_p2g(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                        const R* __restrict__ co, R* __restrict__ gm)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    const R m = co[CO_M * ld + p];
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    walk_rotated<R, K>(sn, [&](int i, int j, int k, R w, R, R, R) {
+        if (in_grid(kp, i, j, k)) atomicAdd(&gm[node_of(kp, i, j, k)], w * m);
+    });
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_loss_sums(long long nn, const R* __restrict__ gm,
+                                                         const R* __restrict__ tm, double* acc)
+{
+    __shared__ double red[32];
+    double a = 0, b = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x) {
+        a += (double)gm[i];
+        b += (double)tm[4 * i + 3];
+    }
+    a = block_sum<R>(a, red);
+    b = block_sum<R>(b, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(&acc[0], a);
+        atomicAdd(&acc[1], b);
+    }
+}
+
+// per-node loss and dL/dm (CompGraph.cpp:60-92)
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_loss_nodes(long long nn, const R* __restrict__ gm,
+                                                          const R* __restrict__ tm, R* __restrict__ dLdm,
+                                                          double* acc)
+{
+    __shared__ double red[32];
+    const double eps = 1e-4, min_mass = 1e-3, eps_s = 1e-6;
+    const double sc = (acc[1] + eps_s) / (acc[0] + eps_s);
+    double loss = 0, gc = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x) {
+        const double c = (double)gm[i];
+        const double cms = sc * c;
+        const double ld = log(cms + 1.0 + eps) - log((double)tm[4 * i + 3] + 1.0 + eps);
+        loss += 0.5 * ld * ld;
+        double gg = ld / (cms + 1.0 + eps);
+        if (cms < min_mass) {
+            const double diff = min_mass - cms;
+            loss += diff * diff;
+            gg += -2.0 * diff;
+        }
+        dLdm[i] = (R)(sc * gg);
+        gc += gg * c;
+    }
+    loss = block_sum<R>(loss, red);
+    gc = block_sum<R>(gc, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(&acc[2], loss);
+        atomicAdd(&acc[3], gc);
+    }
+}
+
+// dL/dx of the last layer (CompGraph.cpp:94-126); zeroes dL/dv, dL/dF, dL/dC
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_loss_grad(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                         const R* __restrict__ co, const R* __restrict__ tm,
+                                                         const R* __restrict__ dLdm, const double* acc,
+                                                         R* __restrict__ g)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    const R m = co[CO_M * ld + p];
+    R corr = R(0);
+    if (kp.exact) {
+        const double eps_s = 1e-6;
+        const double sc = (acc[1] + eps_s) / (acc[0] + eps_s);
+        corr = (R)(acc[3] * (-sc / (acc[0] + eps_s)));
+    }
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, true);
+    R a0 = 0, a1 = 0, a2 = 0;
+    const R nidx = -kp.inv_dx;
+#pragma unroll
+    for (int a = 0; a < K; ++a)
+#pragma unroll
+        for (int b = 0; b < K; ++b)
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                const int i = sn.base[0] + a, j = sn.base[1] + b, k = sn.base[2] + c;
+                if (!in_grid(kp, i, j, k)) continue;
+                const long long nd = node_of(kp, i, j, k);
+                const R pen = (kp.exact || tm[4 * nd + 3] > R(1e-12)) ? R(1) : R(5);
+                const R f = pen * m * (dLdm[nd] + corr);
+                a0 += f * nidx * sn.s[0][a] * sn.w[1][b] * sn.w[2][c];
+                a1 += f * nidx * sn.w[0][a] * sn.s[1][b] * sn.w[2][c];
+                a2 += f * nidx * sn.w[0][a] * sn.w[1][b] * sn.s[2][c];
+            }
+    g[(ST_X + 0) * ld + p] = a0;
+    g[(ST_X + 1) * ld + p] = a1;
+    g[(ST_X + 2) * ld + p] = a2;
+#pragma unroll
+    for (int q = 3; q < ST_N; ++q) g[(long long)q * ld + p] = R(0);
+}
+
+// ------------------------------------------------------------- volumes
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_p2g_plain(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                         const R* __restrict__ co, R* __restrict__ grid)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3], v[3], C[9];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    load_planes(st + ST_V * ld, ld, p, 3, v);
+    load_planes(st + ST_C * ld, ld, p, 9, C);
+    const R m = co[CO_M * ld + p];
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    walk_rotated<R, K>(sn, [&](int i, int j, int k, R w, R gx, R gy, R gz) {
+        if (!in_grid(kp, i, j, k)) return;
+        const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            atomicAdd(&grid[nd * 4 + r], w * (m * v[r] + m * (C[r * 3] * gx + C[r * 3 + 1] * gy + C[r * 3 + 2] * gz)));
+        atomicAdd(&grid[nd * 4 + 3], w * m);
+    });
+}
+
+// CalculatePointCloudVolumes gather (ForwardSimulation.cpp:250-270)
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads) k_volumes(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                       R* __restrict__ co, const R* __restrict__ grid)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    R mg = 0;
+#pragma unroll
+    for (int a = 0; a < K; ++a)
+#pragma unroll
+        for (int b = 0; b < K; ++b)
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                const int i = sn.base[0] + a, j = sn.base[1] + b, k = sn.base[2] + c;
+                if (!in_grid(kp, i, j, k)) continue;
+                mg += sn.w[0][a] * sn.w[1][b] * sn.w[2][c] * grid[node_of(kp, i, j, k) * 4 + 3];
+            }
+    const R cell = kp.dx * kp.dx * kp.dx;
+    const R rho = mg / (cell > R(1e-12) ? cell : R(1e-12));
+    co[CO_VOL * ld + p] = rho > R(1.1920928955078125e-07) ? co[CO_M * ld + p] / rho : R(0);
+}
+
+// ---------------------------------------------------------------- Adam
+
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_sumsq(int n, long long ld, const R* __restrict__ g, int planes,
+                                                     double* acc)
+{
+    __shared__ double red[32];
+    double s = 0;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        for (int q = 0; q < planes; ++q) {
+            const double v = (double)g[(long long)q * ld + p];
+            s += v * v;
+        }
+    s = block_sum<R>(s, red);
+    if (threadIdx.x == 0) atomicAdd(acc, s);
+}
+
+// Descend_Adam (PointCloud.cpp:83-147) with FP64 moments
+template <typename R>
+__global__ void __launch_bounds__(kThreads) k_adam(int n, long long ld, const R* __restrict__ gF, R* __restrict__ dfc,
+                                                    double* __restrict__ mom, double* __restrict__ vec,
+                                                    double* __restrict__ vmax, double alpha, double inv_gn,
+                                                    double beta1, double beta2, double eps, double bc1, double bc2)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    double step[9], xo[9], sn = 0, xn = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const long long k = (long long)i * ld + p;
+        const double g = (double)gF[k] * inv_gn;
+        const double m = beta1 * mom[k] + (1.0 - beta1) * g;
+        const double v = beta2 * vec[k] + (1.0 - beta2) * g * g;
+        mom[k] = m;
+        vec[k] = v;
+        const double vh = v / bc2;
+        const double vm = vh > vmax[k] ? vh : vmax[k];
+        vmax[k] = vm;
+        double den = sqrt(vm);
+        den = den < 1e-8 ? 1e-8 : den;
+        step[i] = (m / bc1) / (den + eps);
+        sn += step[i] * step[i];
+        xo[i] = (double)dfc[k];
+        xn += xo[i] * xo[i];
+    }
+    sn = sqrt(sn);
+    xn = sqrt(xn);
+    double cap = 5e-2 * (xn > 1.0 ? xn : 1.0);
+    cap = cap < 5e-3 ? 5e-3 : cap;
+    double scale = 1.0;
+    if (sn > 0 && alpha * sn > cap) scale = cap / (alpha * sn);
+    double small = 1e-3 * (xn > 1.0 ? xn : 1.0);
+    small = small < 1e-4 ? 1e-4 : small;
+    const bool near = alpha * sn <= small;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        double nx = xo[i] - alpha * step[i] * scale;
+        if (near) nx = xo[i] + 0.2 * (nx - xo[i]);
+        dfc[(long long)i * ld + p] = (R)nx;
+    }
+}
+
+// ------------------------------------------------------------- utility
+
+template <typename R, typename T>
+__global__ void k_aos_to_planes(int n, int k, long long ld, const T* __restrict__ src, R* __restrict__ dst)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int p = (int)(t / k), q = (int)(t % k);
+    dst[(long long)q * ld + p] = (R)src[t];
+}
+
+template <typename R, typename T>
+__global__ void k_planes_to_aos(int n, int k, long long ld, const R* __restrict__ src, T* __restrict__ dst)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int p = (int)(t / k), q = (int)(t % k);
+    dst[t] = (T)src[(long long)q * ld + p];
+}
+
+template <typename R>
+__global__ void k_axpy_planes(int n, int k, long long ld, R alpha, const R* __restrict__ x, R* __restrict__ y)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int q = (int)(t / n), p = (int)(t % n);
+    y[(long long)q * ld + p] += alpha * x[(long long)q * ld + p];
+}
+
+template <typename R>
+__global__ void k_fill_planes(int n, int k, long long ld, R value, R* __restrict__ y)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int q = (int)(t / n), p = (int)(t % n);
+    y[(long long)q * ld + p] = value;
+}
+
+template <typename R>
+__global__ void k_count_active(long long nn, const R* __restrict__ grid, unsigned long long* out)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = i < nn && grid[4 * i + 3] > R(0);
+    unsigned b = __ballot_sync(0xffffffffu, act);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(out, (unsigned long long)__popc(b));
+}
+
+template <typename R>
+__global__ void k_nonfinite(int n, int k, long long ld, const R* __restrict__ y, int* flag)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int q = (int)(t / n), p = (int)(t % n);
+    if (!isfinite((double)y[(long long)q * ld + p])) *flag = 1;
+}
+
+template <typename R>
+int tile_cap_for()
+{
+    // shared float atomics are native; double tiles are not used (the plain
+    // FP64 form scatters with global atomics)
+    return sizeof(R) == 4 ? g_tile_nodes : 0;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------- launchers
+
+template <typename R>
+void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
+                cudaStream_t s)
+{
+    if (n <= 0) return;
+    const int cap = tile_cap_for<R>();
+    const size_t sm = (size_t)cap * 4 * sizeof(R);
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+    else k_p2g<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+}
+
+template <typename R>
+void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s)
+{
+    const long long nn = c.nodes();
+    k_grid_update<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid);
+}
+
+template <typename R>
+void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* grid, R* st1, R* trust,
+                cudaStream_t s)
+{
+    if (n <= 0) return;
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0) k_g2p<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
+    else k_g2p<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
+}
+
+template <typename R>
+void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* st1, const R* g1,
+                    const R* trust, R* adj, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const int cap = tile_cap_for<R>();
+    const size_t sm = (size_t)cap * 3 * sizeof(R);
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0) k_g2p_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+    else k_g2p_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+}
+
+template <typename R>
+void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s)
+{
+    const long long nn = c.nodes();
+    k_grid_adj<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, adj);
+}
+
+template <typename R>
+void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, const R* st1,
+                    const R* g1, const R* trust, const R* grid, const R* adj, R* g, R* gFt, R* glam, R* gmu,
+                    cudaStream_t s)
+{
+    if (n <= 0) return;
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0)
+        k_p2g_adj<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+                                                         glam, gmu);
+    else
+        k_p2g_adj<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+                                                         glam, gmu);
+}
+
+template <typename R>
+void launch_loss(const StepCfg& c, int n, long long ld, const R* st, const R* co, const R* target_m, R* gm, R* dLdm,
+                 double* acc, R* g, cudaStream_t s)
+{
+    const long long nn = c.nodes();
+    auto kp = make_kp<R>(c);
+    cudaMemsetAsync(gm, 0, sizeof(R) * nn, s);
+    cudaMemsetAsync(acc, 0, sizeof(double) * 4, s);
+    if (n > 0) {
+        if (c.kernel == 0) k_mass_p2g<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
+        else k_mass_p2g<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
+    }
+    const int nb = (int)std::min<long long>(nblocks(nn), 1184);
+    k_loss_sums<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, acc);
+    k_loss_nodes<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, dLdm, acc);
+    if (n > 0) {
+        if (c.kernel == 0) k_loss_grad<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, target_m, dLdm, acc, g);
+        else k_loss_grad<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, target_m, dLdm, acc, g);
+    }
+}
+
+template <typename R>
+void launch_p2g_plain(const StepCfg& c, int n, long long ld, const R* st, const R* co, R* grid, cudaStream_t s)
+{
+    if (n <= 0) return;
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0) k_p2g_plain<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
+    else k_p2g_plain<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
+}
+
+template <typename R>
+void launch_volumes(const StepCfg& c, int n, long long ld, const R* st, R* co, const R* grid, cudaStream_t s)
+{
+    if (n <= 0) return;
+    auto kp = make_kp<R>(c);
+    if (c.kernel == 0) k_volumes<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
+    else k_volumes<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
+}
+
+template <typename R>
+void launch_sumsq(int n, long long ld, const R* g, int plane0, int planes, double* acc, cudaStream_t s)
+{
+    cudaMemsetAsync(acc, 0, sizeof(double), s);
+    if (n <= 0) return;
+    const int nb = std::min(nblocks(n), 1184);
+    k_sumsq<R><<<nb, kThreads, 0, s>>>(n, ld, g + (long long)plane0 * ld, planes, acc);
+}
+
+template <typename R>
+void launch_adam(int n, long long ld, const R* gF, R* dfc, double* mom, double* vec, double* vmax, double alpha,
+                 double inv_gn, double beta1, double beta2, double eps, int t, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const double bc1 = 1.0 - pow(beta1, t), bc2 = 1.0 - pow(beta2, t);
+    k_adam<R><<<nblocks(n), kThreads, 0, s>>>(n, ld, gF, dfc, mom, vec, vmax, alpha, inv_gn, beta1, beta2, eps, bc1,
+                                               bc2);
+}
+
+template <typename R, typename T>
+void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_aos_to_planes<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
+}
+
+template <typename R, typename T>
+void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_planes_to_aos<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
+}
+
+template <typename R>
+void launch_axpy_planes(int n, int k, long long ld, R alpha, const R* x, R* y, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_axpy_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, alpha, x, y);
+}
+
+template <typename R>
+void launch_fill_planes(int n, int k, long long ld, R value, R* y, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_fill_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, value, y);
+}
+
+template <typename R>
+void launch_count_active(const StepCfg& c, const R* grid, unsigned long long* out, cudaStream_t s)
+{
+    cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+    const long long nn = c.nodes();
+    k_count_active<R><<<nblocks(nn), kThreads, 0, s>>>(nn, grid, out);
+}
+
+template <typename R>
+void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_nonfinite<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, y, flag);
+}
+
+#define MPM_INSTANTIATE(R)                                                                                         \
+    template void launch_p2g<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, cudaStream_t);   \
+    template void launch_grid_update<R>(const StepCfg&, R*, cudaStream_t);                                         \
+    template void launch_g2p<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, R*, cudaStream_t); \
+    template void launch_g2p_adj<R>(const StepCfg&, int, long long, const R*, const R*, const R*, const R*,        \
+                                    const R*, R*, cudaStream_t);                                                   \
+    template void launch_grid_adj<R>(const StepCfg&, const R*, R*, cudaStream_t);                                  \
+    template void launch_p2g_adj<R>(const StepCfg&, int, long long, const R*, const R*, const R*, const R*,        \
+                                    const R*, const R*, const R*, const R*, R*, R*, R*, R*, cudaStream_t);         \
+    template void launch_loss<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, R*, double*, R*, \
+                                 cudaStream_t);                                                                    \
+    template void launch_p2g_plain<R>(const StepCfg&, int, long long, const R*, const R*, R*, cudaStream_t);       \
+    template void launch_volumes<R>(const StepCfg&, int, long long, const R*, R*, const R*, cudaStream_t);         \
+    template void launch_sumsq<R>(int, long long, const R*, int, int, double*, cudaStream_t);                     \
+    template void launch_adam<R>(int, long long, const R*, R*, double*, double*, double*, double, double, double, \
+                                 double, double, int, cudaStream_t);                                               \
+    template void launch_aos_to_planes<R, float>(int, int, long long, const float*, R*, cudaStream_t);            \
+    template void launch_aos_to_planes<R, double>(int, int, long long, const double*, R*, cudaStream_t);          \
+    template void launch_planes_to_aos<R, float>(int, int, long long, const R*, float*, cudaStream_t);            \
+    template void launch_planes_to_aos<R, double>(int, int, long long, const R*, double*, cudaStream_t);          \
+    template void launch_axpy_planes<R>(int, int, long long, R, const R*, R*, cudaStream_t);                      \
+    template void launch_fill_planes<R>(int, int, long long, R, R*, cudaStream_t);                                \
+    template void launch_count_active<R>(const StepCfg&, const R*, unsigned long long*, cudaStream_t);             \
+    template void launch_nonfinite<R>(int, int, long long, const R*, int*, cudaStream_t);
+
+MPM_INSTANTIATE(float)
+MPM_INSTANTIATE(double)
+
+}  // namespace mpm

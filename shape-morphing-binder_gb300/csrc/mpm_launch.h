@@ -1,0 +1,90 @@
+// mpm_launch.h -- host-side launchers for the MPM kernels (internal header).
+//
+// Particle state of one layer is stored as planes (structure of arrays) of
+// length ld >= n:  x0..x2, v0..v2, C00..C22, F00..F22   (24 planes, STATE_*)
+// Particle constants:  m, vol, lam, mu                  (4 planes,  CONST_*)
+// Control dFc:          9 planes (absent = zero)
+// Layer gradients:      dL/dx, dL/dv, dL/dF, dL/dC       (24 planes, same order)
+// Grid nodes: 4 scalars per node, node (i,j,k) at (i*dy + j)*dz + k
+//   forward grid: (p0,p1,p2,m) after P2G, (v0,v1,v2,m) after the grid update
+//   adjoint grid: (dL/dv0..2, 0) after the G2P transpose, (dL/dp0..2, dL/dm)
+//   after the grid-update transpose.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mpm {
+
+enum { ST_X = 0, ST_V = 3, ST_C = 6, ST_F = 15, ST_N = 24 };
+enum { CO_M = 0, CO_VOL = 1, CO_LAM = 2, CO_MU = 3, CO_N = 4 };
+
+struct StepCfg {
+    double dt = 1.0 / 120.0, drag = 0.5, smoothing = 0.1;
+    double fext[3] = {0, 0, 0};
+    double bulk = 0.25, jmin = 0.6;
+    int dims[3] = {1, 1, 1};
+    double dx = 1.0;
+    double gmin[3] = {0, 0, 0};
+    int kernel = 0;    // 0 cubic B-spline, 1 quadratic
+    int material = 0;  // 0 fixed-corotated, 1 Neo-Hookean
+    int exact = 0;     // 0 reference-compatible adjoint, 1 exact adjoint
+    long long nodes() const { return (long long)dims[0] * dims[1] * dims[2]; }
+};
+
+// Shared-memory tile budget (nodes) for the scatter kernels; 0 disables tiles.
+extern int g_tile_nodes;
+
+template <typename R>
+void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
+                cudaStream_t s);
+template <typename R>
+void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s);
+template <typename R>
+void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* grid, R* st1, R* trust,
+                cudaStream_t s);
+// adjoint: G2P^T scatter (+P_op_2^T), grid update^T, P2G^T gather (+P_op_1^T)
+template <typename R>
+void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* st1, const R* g1,
+                    const R* trust, R* adj, cudaStream_t s);
+template <typename R>
+void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s);
+template <typename R>
+void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, const R* st1,
+                    const R* g1, const R* trust, const R* grid, const R* adj, R* g, R* gFt, R* glam, R* gmu,
+                    cudaStream_t s);
+
+// mass loss (CompGraph.cpp:42-129).  target: a grid (4 scalars per node, mass
+// in slot 3); acc: 4 doubles (sum_c, sum_t, loss, sum g*c)
+template <typename R>
+void launch_loss(const StepCfg& c, int n, long long ld, const R* st, const R* co, const R* target_m, R* gm, R* dLdm,
+                 double* acc, R* g, cudaStream_t s);
+
+// P2G with dt = drag = 0 into an un-reset grid, and the volume gather
+template <typename R>
+void launch_p2g_plain(const StepCfg& c, int n, long long ld, const R* st, const R* co, R* grid, cudaStream_t s);
+template <typename R>
+void launch_volumes(const StepCfg& c, int n, long long ld, const R* st, R* co, const R* grid, cudaStream_t s);
+
+// Adam over one layer's control (PointCloud.cpp:83-147); sumsq of dL/dF
+template <typename R>
+void launch_sumsq(int n, long long ld, const R* g, int plane0, int planes, double* acc, cudaStream_t s);
+template <typename R>
+void launch_adam(int n, long long ld, const R* gF, R* dfc, double* mom, double* vec, double* vmax, double alpha,
+                 double inv_gn, double beta1, double beta2, double eps, int t, cudaStream_t s);
+
+// layout conversion: (n, k) row-major <-> k planes of stride ld
+template <typename R, typename T>
+void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s);
+template <typename R, typename T>
+void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s);
+template <typename R>
+void launch_axpy_planes(int n, int k, long long ld, R alpha, const R* x, R* y, cudaStream_t s);
+template <typename R>
+void launch_fill_planes(int n, int k, long long ld, R value, R* y, cudaStream_t s);
+// count of nonzero-mass nodes (for the roofline's active-node bytes)
+template <typename R>
+void launch_count_active(const StepCfg& c, const R* grid, unsigned long long* out, cudaStream_t s);
+// non-finite check over planes; sets *flag = 1 on NaN/Inf
+template <typename R>
+void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStream_t s);
+
+}  // namespace mpm

@@ -1,0 +1,443 @@
+// mpm_math.cuh -- per-particle device math for the MPM step and its adjoint.
+//
+// 3x3 matrices are row-major arrays of 9 scalars.  Everything is templated on
+// the storage scalar R (float for the production path, double for the plain
+// all-FP64 form).  The float path computes the polar decomposition with a
+// scaled Newton iteration in FP32 and falls back to an FP64 Jacobi SVD when
+// F is close to inversion (the FP64 guard); J - 1 is formed from F - I so the
+// volumetric stress does not lose digits to cancellation.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#define MPM_HD __host__ __device__ __forceinline__
+#define MPM_D __device__ __forceinline__
+
+namespace mpm {
+
+// ---------------------------------------------------------------- 3x3 ops
+
+template <typename R>
+MPM_HD R det3(const R* A)
+{
+    return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+           A[2] * (A[3] * A[7] - A[4] * A[6]);
+}
+
+// cofactor matrix cof(A) = det(A) A^{-T}
+template <typename R>
+MPM_HD void cof3(const R* A, R* c)
+{
+    c[0] = A[4] * A[8] - A[5] * A[7];
+    c[1] = A[5] * A[6] - A[3] * A[8];
+    c[2] = A[3] * A[7] - A[4] * A[6];
+    c[3] = A[2] * A[7] - A[1] * A[8];
+    c[4] = A[0] * A[8] - A[2] * A[6];
+    c[5] = A[1] * A[6] - A[0] * A[7];
+    c[6] = A[1] * A[5] - A[2] * A[4];
+    c[7] = A[2] * A[3] - A[0] * A[5];
+    c[8] = A[0] * A[4] - A[1] * A[3];
+}
+
+template <typename R>
+MPM_HD void mul3(const R* A, const R* B, R* C)  // C = A B
+{
+    R t[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) t[r * 3 + c] = A[r * 3] * B[c] + A[r * 3 + 1] * B[3 + c] + A[r * 3 + 2] * B[6 + c];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = t[i];
+}
+
+template <typename R>
+MPM_HD void mulTN3(const R* A, const R* B, R* C)  // C = A^T B
+{
+    R t[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) t[r * 3 + c] = A[r] * B[c] + A[3 + r] * B[3 + c] + A[6 + r] * B[6 + c];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = t[i];
+}
+
+template <typename R>
+MPM_HD void mulNT3(const R* A, const R* B, R* C)  // C = A B^T
+{
+    R t[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            t[r * 3 + c] = A[r * 3] * B[c * 3] + A[r * 3 + 1] * B[c * 3 + 1] + A[r * 3 + 2] * B[c * 3 + 2];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) C[i] = t[i];
+}
+
+template <typename R>
+MPM_HD R dot9(const R* A, const R* B)
+{
+    R s = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) s += A[i] * B[i];
+    return s;
+}
+
+// det(F) - 1 through D = F - I (no cancellation for F near I)
+template <typename R>
+MPM_HD R det_minus_one(const R* F)
+{
+    R d0 = F[0] - R(1), d4 = F[4] - R(1), d8 = F[8] - R(1);
+    R tr = d0 + d4 + d8;
+    R m2 = (d0 * d4 - F[1] * F[3]) + (d0 * d8 - F[2] * F[6]) + (d4 * d8 - F[5] * F[7]);
+    R D[9] = {d0, F[1], F[2], F[3], d4, F[5], F[6], F[7], d8};
+    return tr + m2 + det3(D);
+}
+
+// ------------------------------------------------------------- B-splines
+
+// cubic B-spline N(x) and N'(x), DiffMPMLib3D/Interpolation.h:5-30
+template <typename R>
+MPM_HD R cubic_w(R x, R& slope)
+{
+    R ax = fabs(x);
+    if (ax < R(1)) {
+        slope = R(1.5) * x * ax - R(2) * x;
+        return R(0.5) * ax * ax * ax - ax * ax + R(2) / R(3);
+    }
+    if (ax < R(2)) {
+        R t = R(2) - ax;
+        slope = -x * ax / R(2) + R(2) * x - R(2) * x / ax;
+        return t * t * t / R(6);
+    }
+    slope = R(0);
+    return R(0);
+}
+
+// quadratic B-spline (optional kernel)
+template <typename R>
+MPM_HD R quad_w(R x, R& slope)
+{
+    R ax = fabs(x);
+    if (ax < R(0.5)) {
+        slope = R(-2) * x;
+        return R(0.75) - x * x;
+    }
+    if (ax < R(1.5)) {
+        R t = R(1.5) - ax;
+        slope = x > R(0) ? -t : t;
+        return R(0.5) * t * t;
+    }
+    slope = R(0);
+    return R(0);
+}
+
+// Per-particle stencil: base node index and per-axis weights, slopes and
+// offsets dg = x_node - x_p (node position min + i*dx as in Grid.cpp:7-26).
+template <typename R, int K>
+struct Stencil {
+    int base[3];
+    R w[3][K];
+    R s[3][K];
+    R g[3][K];
+};
+
+template <typename R, int K>
+MPM_HD void make_stencil(const R* x, const R* gmin, R dx, R inv_dx, Stencil<R, K>& st, bool want_slope)
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        R rel = (x[a] - gmin[a]) / dx;
+        int b = (K == 4) ? (int)floor(rel) - 1 : (int)floor(rel - R(0.5));
+        st.base[a] = b;
+#pragma unroll
+        for (int o = 0; o < K; ++o) {
+            R node = gmin[a] + R(b + o) * dx;
+            R dg = node - x[a];
+            R sl;
+            st.g[a][o] = dg;
+            st.w[a][o] = (K == 4) ? cubic_w(dg / dx, sl) : quad_w(dg / dx, sl);
+            st.s[a][o] = want_slope ? sl : R(0);
+        }
+    }
+}
+
+// ------------------------------------------------------------ polar / SVD
+
+// cyclic Jacobi eigen-decomposition of a symmetric matrix (double)
+MPM_HD void sym_eig3(const double* Ain, double* w, double* V)
+{
+    double A[9];
+    for (int i = 0; i < 9; ++i) {
+        A[i] = Ain[i];
+        V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    }
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+        double diag = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+        if (off <= 1e-300 || off <= 1e-34 * diag) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                double apq = A[p * 3 + q];
+                if (apq == 0.0) continue;
+                double app = A[p * 3 + p], aqq = A[q * 3 + q];
+                double theta = (aqq - app) / (2.0 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                A[p * 3 + p] = app - t * apq;
+                A[q * 3 + q] = aqq + t * apq;
+                A[p * 3 + q] = A[q * 3 + p] = 0.0;
+                int r = 3 - p - q;
+                double arp = A[r * 3 + p], arq = A[r * 3 + q];
+                A[r * 3 + p] = A[p * 3 + r] = c * arp - s * arq;
+                A[r * 3 + q] = A[q * 3 + r] = s * arp + c * arq;
+                for (int k = 0; k < 3; ++k) {
+                    double vkp = V[k * 3 + p], vkq = V[k * 3 + q];
+                    V[k * 3 + p] = c * vkp - s * vkq;
+                    V[k * 3 + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    w[0] = A[0];
+    w[1] = A[4];
+    w[2] = A[8];
+}
+
+// Rotation-variant polar factor through an SVD (double): R = U V^T, det R = +1,
+// the sign of det F carried by the smallest singular value.
+MPM_HD void polar_svd(const double* F, double* Rm)
+{
+    double FtF[9], w[3], V[9];
+    mulTN3(F, F, FtF);
+    sym_eig3(FtF, w, V);
+    int o0 = 0, o1 = 1, o2 = 2, t;
+    if (w[o1] > w[o0]) { t = o0; o0 = o1; o1 = t; }
+    if (w[o2] > w[o0]) { t = o0; o0 = o2; o2 = t; }
+    if (w[o2] > w[o1]) { t = o1; o1 = o2; o2 = t; }
+    int ord[3] = {o0, o1, o2};
+    double Vs[9];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) Vs[r * 3 + c] = V[r * 3 + ord[c]];
+    if (det3(Vs) < 0)
+        for (int r = 0; r < 3; ++r) Vs[r * 3 + 2] = -Vs[r * 3 + 2];
+    double u[3][3];
+    for (int c = 0; c < 2; ++c)
+        for (int r = 0; r < 3; ++r) u[c][r] = F[r * 3] * Vs[c] + F[r * 3 + 1] * Vs[3 + c] + F[r * 3 + 2] * Vs[6 + c];
+    double n1 = sqrt(u[0][0] * u[0][0] + u[0][1] * u[0][1] + u[0][2] * u[0][2]);
+    if (n1 > 1e-300) {
+        for (int r = 0; r < 3; ++r) u[0][r] /= n1;
+    } else {
+        u[0][0] = 1; u[0][1] = 0; u[0][2] = 0;
+    }
+    double d = u[0][0] * u[1][0] + u[0][1] * u[1][1] + u[0][2] * u[1][2];
+    for (int r = 0; r < 3; ++r) u[1][r] -= d * u[0][r];
+    double n2 = sqrt(u[1][0] * u[1][0] + u[1][1] * u[1][1] + u[1][2] * u[1][2]);
+    if (n2 > 1e-14 * (n1 > 1e-300 ? n1 : 1.0)) {
+        for (int r = 0; r < 3; ++r) u[1][r] /= n2;
+    } else {
+        int k = (fabs(u[0][0]) < fabs(u[0][1])) ? (fabs(u[0][0]) < fabs(u[0][2]) ? 0 : 2)
+                                                 : (fabs(u[0][1]) < fabs(u[0][2]) ? 1 : 2);
+        double e[3] = {0, 0, 0};
+        e[k] = 1;
+        double dd = e[0] * u[0][0] + e[1] * u[0][1] + e[2] * u[0][2];
+        for (int r = 0; r < 3; ++r) u[1][r] = e[r] - dd * u[0][r];
+        double nn = sqrt(u[1][0] * u[1][0] + u[1][1] * u[1][1] + u[1][2] * u[1][2]);
+        for (int r = 0; r < 3; ++r) u[1][r] /= nn;
+    }
+    u[2][0] = u[0][1] * u[1][2] - u[0][2] * u[1][1];
+    u[2][1] = u[0][2] * u[1][0] - u[0][0] * u[1][2];
+    u[2][2] = u[0][0] * u[1][1] - u[0][1] * u[1][0];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Rm[r * 3 + c] = u[0][r] * Vs[c * 3] + u[1][r] * Vs[c * 3 + 1] + u[2][r] * Vs[c * 3 + 2];
+}
+
+template <typename R>
+struct Tol;
+template <>
+struct Tol<float> {
+    static constexpr float newton = 1e-13f;  // squared relative step
+    static constexpr int iters = 12;
+};
+template <>
+struct Tol<double> {
+    static constexpr double newton = 1e-30;
+    static constexpr int iters = 40;
+};
+
+// Scaled Newton iteration for the polar factor (Higham 1986):
+// X <- (g X + X^{-T} / g) / 2, g = sqrt(|X^{-1}|_F / |X|_F) while far away.
+// Returns false when the iterate becomes singular or does not converge.
+template <typename R>
+MPM_HD bool polar_newton(const R* F, R* Rm)
+{
+    R X[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) X[i] = F[i];
+    bool scale = true;
+    for (int it = 0; it < Tol<R>::iters; ++it) {
+        R c[9];
+        cof3(X, c);
+        R d = X[0] * c[0] + X[1] * c[1] + X[2] * c[2];
+        if (!(d > R(0))) return false;
+        R inv_d = R(1) / d;
+        R g = R(1), ig = R(1);
+        if (scale) {
+            R nx = dot9(X, X), nc = dot9(c, c) * inv_d * inv_d;
+            g = sqrt(sqrt(nc / nx));
+            ig = R(1) / g;
+        }
+        R diff = 0, ny = 0;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            R y = R(0.5) * (g * X[i] + c[i] * inv_d * ig);
+            R e = y - X[i];
+            diff += e * e;
+            ny += y * y;
+            X[i] = y;
+        }
+        if (diff < R(1e-4)) scale = false;
+        if (diff <= Tol<R>::newton * ny) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Rm[i] = X[i];
+            return true;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Rm[i] = X[i];
+    return true;
+}
+
+// F = R S.  The FP32 path uses Newton when F is safely away from inversion
+// and the FP64 SVD otherwise (the FP64 guard).
+template <typename R>
+MPM_HD void polar(const R* F, R* Rm, R* S)
+{
+    R J = det3(F);
+    R n2 = dot9(F, F);
+    R ref = n2 * sqrt(n2) * R(0.19245008972987526);  // (|F|_F / sqrt 3)^3
+    bool ok = (J > R(0.05) * ref) && polar_newton(F, Rm);
+    if (!ok) {
+        double Fd[9], Rd[9];
+        for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
+        polar_svd(Fd, Rd);
+        for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+    }
+    R RtF[9];
+    mulTN3(Rm, F, RtF);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S[r * 3 + c] = R(0.5) * (RtF[r * 3 + c] + RtF[c * 3 + r]);
+}
+
+// --------------------------------------------------------- constitutive
+
+enum { MAT_FCR = 0, MAT_NEOHOOKEAN = 1 };
+
+// Invariants shared by P and its VJP.  Jraw = det F, Jc = max(Jraw, 1e-6),
+// Jm1c = Jc - 1 (from F - I when Jraw is not clamped), Fit = F^{-T}.
+// Below J = 0.25 (near inversion) these are formed in FP64.
+template <typename R>
+struct Inv {
+    R Jraw, Jc, Jm1c;
+    R Fit[9];
+};
+
+template <typename R>
+MPM_HD void invariants(const R* F, Inv<R>& v)
+{
+    R jm1 = det_minus_one(F);
+    R J = R(1) + jm1;
+    if (J > R(0.25)) {
+        R c[9];
+        cof3(F, c);
+        R inv = R(1) / J;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) v.Fit[i] = c[i] * inv;
+        v.Jraw = J;
+        v.Jc = J;
+        v.Jm1c = jm1;
+    } else {
+        double Fd[9], c[9];
+        for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
+        cof3(Fd, c);
+        double Jd = Fd[0] * c[0] + Fd[1] * c[1] + Fd[2] * c[2];
+        for (int i = 0; i < 9; ++i) v.Fit[i] = (R)(c[i] / Jd);
+        double Jcd = Jd > 1e-6 ? Jd : 1e-6;
+        v.Jraw = (R)Jd;
+        v.Jc = (R)Jcd;
+        v.Jm1c = (R)(Jcd - 1.0);
+    }
+}
+
+// P(F): FCR (Elasticity.cpp:45-55) or Neo-Hookean.  R/S are returned for reuse.
+template <typename R>
+MPM_HD void pk(int material, const R* F, R lam, R mu, const Inv<R>& iv, R* P, R* Rm, R* S)
+{
+    if (material == MAT_FCR) {
+        polar(F, Rm, S);
+        R k = lam * iv.Jm1c * iv.Jc;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) P[i] = R(2) * mu * (F[i] - Rm[i]) + k * iv.Fit[i];
+    } else {
+        R lj = log(iv.Jc);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) P[i] = mu * (F[i] - iv.Fit[i]) + lam * lj * iv.Fit[i];
+    }
+}
+
+// VJP of P(F) applied to G = dL/dP; returns dL/dF.  exact == false follows
+// d2_FCE_psi_dF2_mult_by_dF (Elasticity.cpp:57-117), including its use of
+// the clamped J next to the unclamped one inside d(J F^{-T})/dF.
+template <typename R>
+MPM_HD void pk_vjp(int material, bool exact, const R* F, R lam, R mu, const Inv<R>& iv, const R* Rm, const R* S,
+                   const R* G, R* out)
+{
+    const R* Fit = iv.Fit;
+    R fg = dot9(Fit, G);
+    R t[9], sw[9];
+    mulNT3(Fit, G, t);  // Fit G^T
+    mul3(t, Fit, sw);   // Fit G^T Fit
+    if (material == MAT_FCR) {
+        if (!exact || iv.Jraw > R(1e-6)) {
+            R a = lam * iv.Jc * iv.Jc * fg + lam * iv.Jm1c * iv.Jraw * fg;
+            R b = lam * iv.Jm1c * iv.Jraw;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) out[i] = R(2) * mu * G[i] + a * Fit[i] - b * sw[i];
+        } else {
+            R b = lam * iv.Jm1c * iv.Jc;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) out[i] = R(2) * mu * G[i] - b * sw[i];
+        }
+        // -2 mu dR: (tr S I - S) w = axial(R^T G - G^T R), dR = R [w]x
+        R A[9] = {S[4] + S[8], -S[1], -S[2], -S[1], S[0] + S[8], -S[5], -S[2], -S[5], S[0] + S[4]};
+        if (fabs(det3(A)) < R(1e-6)) {
+            A[0] += R(1e-4);
+            A[4] += R(1e-4);
+            A[8] += R(1e-4);
+        }
+        R rg[9];
+        mulTN3(Rm, G, rg);
+        R b3[3] = {rg[7] - rg[5], rg[2] - rg[6], rg[3] - rg[1]};
+        R c[9];
+        cof3(A, c);
+        R idet = R(1) / (A[0] * c[0] + A[1] * c[1] + A[2] * c[2]);
+        R w0 = (c[0] * b3[0] + c[3] * b3[1] + c[6] * b3[2]) * idet;
+        R w1 = (c[1] * b3[0] + c[4] * b3[1] + c[7] * b3[2]) * idet;
+        R w2 = (c[2] * b3[0] + c[5] * b3[1] + c[8] * b3[2]) * idet;
+        R W[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
+        R dR[9];
+        mul3(Rm, W, dR);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] -= R(2) * mu * dR[i];
+    } else {
+        R lj = log(iv.Jc);
+        R kk = (iv.Jraw > R(1e-6)) ? lam * fg : R(0);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) out[i] = mu * G[i] + (mu - lam * lj) * sw[i] + kk * Fit[i];
+    }
+}
+
+}  // namespace mpm

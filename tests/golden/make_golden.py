@@ -1,0 +1,120 @@
+"""Generate golden vectors from the reference's own DiffMPMLib3D sources.
+
+Runs where the reference tree is mounted: it builds oracle/_ref/libref{32,64}.so
+(oracle/build_oracle.py) and records, for small seeded inputs, the outputs of
+the reference's ForwardTimeStep, Back_Timestep, EndLayerMassLoss,
+Descend_Adam, CalculatePointCloudVolumes, PK_FixedCorotatedElasticity and
+d2_FCE_psi_dF2_mult_by_dF, plus a 5-step full-tape forward/backward through
+CompGraph.  The fixtures (tests/golden/*.npz) travel with the repository;
+the GPU tests compare against them without the reference present.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT / "oracle"))
+sys.path.insert(0, str(ROOT / "shape-morphing-binder_gb300"))
+
+import build_oracle  # noqa: E402
+import oracle as O  # noqa: E402
+from diffmpm_bindings import workloads as W  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def small_state(seed=7, G=10, rng_scale=1.0):
+    w = W.sphere32(seed=seed, G=G)
+    rng = np.random.default_rng(seed + 100)
+    n = w.n
+    C0 = 0.5 * rng.normal(size=(n, 3, 3)) * rng_scale
+    F0 = np.eye(3) + 0.04 * rng.normal(size=(n, 3, 3))
+    dFc = 0.01 * rng.normal(size=(n, 3, 3))
+    s = O.State(w.x, w.v, C0, F0, w.m, w.vol, w.lam, w.mu, dFc)
+    return w, s, rng
+
+
+def main():
+    build_oracle.build_oracle()
+    outs = build_oracle.build_ref()
+    if not outs:
+        raise SystemExit("reference tree not found; golden vectors need the reference sources")
+    r64, r32 = O.Reference(64), O.Reference(32)
+    w, s, rng = small_state()
+    g = O.Grid(w.dims, w.dx)
+    prm = O.Params(dt=1e-3, drag=0.5, smoothing=0.1)
+    n = s.n
+    rec = dict(dims=np.asarray(w.dims), dx=w.dx, gmin=np.zeros(3), dt=prm.dt, drag=prm.drag, smoothing=prm.smoothing,
+               x=s.x, v=s.v, C=s.C, F=s.F, dFc=s.dFc, m=s.m, vol=s.vol, lam=s.lam, mu=s.mu)
+    # forward step
+    for bits, ref in ((64, r64), (32, r32)):
+        s1, gstep = ref.forward_step(g, prm, s)
+        for k in ("x", "v", "C", "F"):
+            rec[f"fwd{bits}_{k}"] = getattr(s1, k)
+        rec[f"fwd{bits}_gm"] = gstep["m"]
+        rec[f"fwd{bits}_gv"] = gstep["v"]
+    # backward step (upstream grads seeded)
+    s1, gstep = r64.forward_step(g, prm, s)
+    g1 = O.Grads(rng.normal(size=(n, 3)), rng.normal(size=(n, 3)), 0.1 * rng.normal(size=(n, 3, 3)),
+                 0.01 * rng.normal(size=(n, 3, 3)))
+    rec.update(bwd_C1=s1.C, bwd_gm=gstep["m"], bwd_gv=gstep["v"], bwd_gx1=g1.x, bwd_gv1=g1.v, bwd_gF1=g1.F,
+               bwd_gC1=g1.C)
+    for bits, ref in ((64, r64), (32, r32)):
+        gb = ref.backward_step(g, prm, s, s1.C, gstep, g1)
+        for k in ("x", "v", "F", "C"):
+            rec[f"bwd{bits}_g{k}"] = getattr(gb, k)
+    # mass loss against a target made from shifted particles
+    tgt = np.zeros(g.n_nodes)
+    O.Oracle().p2g_accumulate(g, s1.x + 0.03, s1.v, s1.C, s.m, tgt, np.zeros((g.n_nodes, 3)))
+    rec["loss_target"] = tgt
+    for bits, ref in ((64, r64), (32, r32)):
+        loss, d = ref.mass_loss(g, s1.x, s.m, tgt)
+        rec[f"loss{bits}"] = loss
+        rec[f"loss{bits}_gx"] = d["gx"]
+        rec[f"loss{bits}_dLdm"] = d["dLdm"]
+    # Adam, three steps
+    gF = 0.1 * rng.normal(size=(n, 3, 3))
+    rec["adam_gF"] = gF
+    for bits, ref in ((64, r64), (32, r32)):
+        dFc, mom, vec, vmax = s.dFc.copy(), np.zeros((n, 3, 3)), np.zeros((n, 3, 3)), np.zeros((n, 3, 3))
+        for t in (1, 2, 3):
+            ref.adam(gF * t, dFc, mom, vec, vmax, 0.05, timestep=t)
+        rec[f"adam{bits}_dFc"] = dFc
+        rec[f"adam{bits}_vmax"] = vmax
+    # volumes into an empty grid
+    for bits, ref in ((64, r64), (32, r32)):
+        gm, gp = np.zeros(g.n_nodes), np.zeros((g.n_nodes, 3))
+        rec[f"vol{bits}"] = ref.volumes(g, s.x, s.v, s.C, s.m, gm, gp)
+        rec[f"vol{bits}_gm"] = gm
+        rec[f"vol{bits}_gp"] = gp
+    # constitutive, including inverted and near-singular F
+    Fs = [np.eye(3) + 0.3 * rng.normal(size=(3, 3)) for _ in range(20)]
+    Fs += [rng.normal(size=(3, 3)) for _ in range(10)]
+    Fs += [np.diag([1.0, 1.0, -0.5]), np.diag([2.0, 0.5, 1e-3])]
+    dFs = [rng.normal(size=(3, 3)) for _ in Fs]
+    rec["cons_F"] = np.asarray(Fs)
+    rec["cons_dF"] = np.asarray(dFs)
+    rec["cons_P64"] = np.asarray([r64.pk(F, 5769.23, 3846.15) for F in Fs])
+    rec["cons_H64"] = np.asarray([r64.hvp(F, 5769.23, 3846.15, d) for F, d in zip(Fs, dFs)])
+    # 5-step full-tape rollout through CompGraph (stable density, smoothing on)
+    prm_r = O.Params(dt=1e-3, drag=0.5, smoothing=0.1)
+    s0 = O.State(s.x, s.v, np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), s.m, s.vol, s.lam, s.mu, s.dFc)
+    seed = 2.0 * (s.x - (s.x + 0.02)) / n
+    rec["roll_T"] = 5
+    rec["roll_seed"] = seed
+    for bits, ref in ((64, r64), (32, r32)):
+        xT, gr, _ = ref.rollout(g, prm_r, s0, 5, seed)
+        rec[f"roll{bits}_xT"] = xT
+        for k in ("x", "v", "F", "C"):
+            rec[f"roll{bits}_g{k}"] = getattr(gr, k)
+    np.savez_compressed(OUT / "reference_small.npz", **rec)
+    print("wrote", OUT / "reference_small.npz", "N =", n)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,97 @@
+"""Shared helpers for the parity tests (test infrastructure)."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def rel_err(a, b):
+    """max |a - b| / max |b| (0 when both vanish)."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    den = np.abs(b).max()
+    return float(np.abs(a - b).max() / den) if den > 0 else float(np.abs(a).max())
+
+
+def norm_err(a, b):
+    """||a - b|| / ||b||."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a))
+
+
+def golden_state(gd):
+    import oracle as O
+    return O.State(gd["x"], gd["v"], gd["C"], gd["F"], gd["m"], gd["vol"], gd["lam"], gd["mu"], gd["dFc"])
+
+
+def golden_grid(gd):
+    import oracle as O
+    return O.Grid(tuple(int(d) for d in gd["dims"]), float(gd["dx"]), tuple(gd["gmin"]))
+
+
+def golden_params(gd, exact=False):
+    import oracle as O
+    return O.Params(dt=float(gd["dt"]), drag=float(gd["drag"]), smoothing=float(gd["smoothing"]), exact=exact)
+
+
+def make_graph(dm, s, grid, prm, precision="fp32", adjoint="reference", layers=2, checkpoint_every=1,
+               kernel="cubic", material="fcr", target_mass=None):
+    """CompGraph on the GPU holding state s in layer 0 (oracle.State)."""
+    dtype = np.float64 if precision == "fp64" else np.float32
+    pc = dm.PointCloud.from_arrays(s.x.astype(dtype), v=s.v.astype(dtype), F=s.F.astype(dtype),
+                                   dFc=None if s.dFc is None else s.dFc.astype(dtype), C_=s.C.astype(dtype),
+                                   m=s.m.astype(dtype), vol=s.vol.astype(dtype), lam=s.lam.astype(dtype),
+                                   mu=s.mu.astype(dtype), precision=precision)
+    g = dm.Grid(*grid.dims, grid.dx, grid.min, precision=precision)
+    tg = dm.Grid(*grid.dims, grid.dx, grid.min, precision=precision)
+    if target_mass is not None:
+        tg.set_node_masses(target_mass)
+    cg = dm.CompGraph(pc, g, tg, adjoint=adjoint, kernel=kernel, material=material,
+                      checkpoint_every=checkpoint_every)
+    cg.set_sim_params(dt=prm.dt, drag=prm.drag, smoothing=prm.smoothing, f_ext=prm.f_ext,
+                      bulk_viscosity=prm.bulk_visc, j_min=prm.j_min)
+    cg.set_up_comp_graph(layers)
+    return cg, (pc, g, tg)
+
+
+def layer_state(cg, i, dtype=np.float64):
+    pc = cg.get_point_cloud(i)
+    return {k: pc.get(k, dtype) for k in ("x", "v", "C", "F")}
+
+
+def set_grads(cg, layer, g1):
+    pc = cg.get_point_cloud(layer)
+    pc.set("grad_x", g1.x)
+    pc.set("grad_v", g1.v)
+    pc.set("grad_F", g1.F)
+    pc.set("grad_C", g1.C)
+
+
+def get_grads(cg, layer, dtype=np.float64):
+    pc = cg.get_point_cloud(layer)
+    return {k: pc.get("grad_" + k, dtype) for k in ("x", "v", "F", "C")}
+
+
+def oracle_rollout(orc, grid, prm, s0, T, seed_gx, want_ctl=True):
+    """Forward T steps and the adjoint with the oracle; returns (x_T, layer-0
+    grads incl. the control gradient)."""
+    import oracle as O
+    states, steps = [s0], []
+    s = s0
+    for _ in range(T):
+        s1, st = orc.forward_step(grid, prm, s)
+        states.append(s1)
+        steps.append(st)
+        s = s1
+    n = s0.n
+    g = O.Grads(np.asarray(seed_gx, np.float64).reshape(n, 3).copy(), np.zeros((n, 3)), np.zeros((n, 3, 3)),
+                np.zeros((n, 3, 3)))
+    for t in range(T - 1, -1, -1):
+        g = orc.backward_step(grid, prm, states[t], states[t + 1].C, steps[t], g, want_ft=want_ctl and t == 0)
+    return states[-1].x, g
+
+
+def oracle_loss(orc, grid, prm, s0, T, seed_gx):
+    s = s0
+    for _ in range(T):
+        s, _ = orc.forward_step(grid, prm, s)
+    return float((np.asarray(seed_gx).reshape(-1, 3) * s.x).sum())
