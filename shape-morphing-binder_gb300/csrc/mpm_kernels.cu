@@ -154,7 +154,10 @@ struct Scatter {
             b2 = box[2];
             long long x0 = (long long)box[3] - box[0] + K, x1 = (long long)box[4] - box[1] + K,
                       x2 = (long long)box[5] - box[2] + K;
-            long long v = x0 * x1 * x2;
+            // each extent is checked first so the product cannot overflow
+            // (positions that are Inf/NaN give extents near 2^32)
+            const bool small = x0 > 0 && x1 > 0 && x2 > 0 && x0 <= tile_cap && x1 <= tile_cap && x2 <= tile_cap;
+            const long long v = small ? x0 * x1 * x2 : (long long)tile_cap + 1;
             if (v <= tile_cap) {
                 tile = true;
                 e0 = (int)x0;

@@ -235,14 +235,21 @@ class Grid:
     """Grid(dim_x, dim_y, dim_z, dx, min_point) (Grid.cpp:7-26; bind.cpp:159-160)."""
 
     def __init__(self, dim_x, dim_y, dim_z, dx, min_point, precision=None):
-        mn = np.asarray(_vec3(min_point), dtype=np.float64)
+        prec = _prec(precision)
+        # dx and min_point are float in the reference (Grid.h:96-100): an FP32
+        # grid keeps their float32 values, an FP64 grid the exact ones
+        if prec == MPM_FP64:
+            mn = np.asarray(min_point, dtype=np.float64).reshape(3).copy()
+            dxv = float(dx)
+        else:
+            mn = np.asarray(_vec3(min_point), dtype=np.float64)
+            dxv = float(np.float32(dx))
         h = C.c_void_p()
-        # dx and min are float in the reference; keep their float32 values
-        check(lib.mpm_grid_create(int(dim_x), int(dim_y), int(dim_z), float(np.float32(dx)),
-                                  mn.ctypes.data_as(_lib._dp), _prec(precision), C.byref(h)), "Grid")
+        check(lib.mpm_grid_create(int(dim_x), int(dim_y), int(dim_z), dxv, mn.ctypes.data_as(_lib._dp), prec,
+                                  C.byref(h)), "Grid")
         self._h = h
         self.dims = (int(dim_x), int(dim_y), int(dim_z))
-        self.dx = float(np.float32(dx))
+        self.dx = dxv
         self.min_point = mn.copy()
 
     def __del__(self):
@@ -396,7 +403,8 @@ class CompGraph:
     def end_layer_mass_loss(self) -> float:
         out = C.c_double()
         check(lib.mpm_compgraph_mass_loss(self._h, C.byref(out)), "end_layer_mass_loss")
-        return float(np.float32(out.value))
+        # the reference returns a float; the FP64 engine returns its double
+        return out.value if self.precision == MPM_FP64 else float(np.float32(out.value))
 
     @staticmethod
     def _render_arrays(dLdF_render, dLdx_render, verb):

@@ -1,0 +1,265 @@
+"""GPU tests of the engine features around the step: checkpointed rollouts,
+finite-difference gradients of the FP64 form, shared-tile vs global-atomic
+scatter, the optional kernel/material, CompGraph semantics (render
+gradients, optimisation, promotion), edge cases and the autograd rollout."""
+import copy
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import get_grads, layer_state, make_graph, norm_err, oracle_rollout, rel_err, set_grads
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed=0, G=12, rho=60.0, smoothing=0.0, drag=0.0):
+    from diffmpm_bindings import workloads as W
+    w = W.sphere32(seed=seed, G=G, rho=rho)
+    rng = np.random.default_rng(seed)
+    n = w.n
+    s0 = O.State(w.x, w.v, 0.05 * rng.normal(size=(n, 3, 3)), np.eye(3) + 0.02 * rng.normal(size=(n, 3, 3)),
+                 w.m, w.vol, w.lam, w.mu, 0.01 * rng.normal(size=(n, 3, 3)))
+    g = O.Grid(w.dims, w.dx)
+    return s0, g, rng, smoothing, drag
+
+
+def _rollout(dm, s0, g, prm, T, seed_gx, precision, adjoint="exact", checkpoint_every=1, **kw):
+    cg, keep = make_graph(dm, s0, g, prm, precision=precision, adjoint=adjoint, layers=T + 1,
+                          checkpoint_every=checkpoint_every, **kw)
+    cg.compute_forward_pass(0, 0)
+    n = s0.n
+    last = cg.get_point_cloud(T)
+    last.set("grad_x", seed_gx)
+    last.set("grad_v", np.zeros((n, 3)))
+    last.set("grad_F", np.zeros((n, 3, 3)))
+    last.set("grad_C", np.zeros((n, 3, 3)))
+    cg.compute_backward_pass(0)
+    xT = last.get("x", np.float64)
+    g0 = get_grads(cg, 0)
+    g0["dFc"] = cg.get_grad(0, "dFc", np.float64)
+    return xT, g0, cg, keep
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_multistep_exact_matches_oracle(dm, orc, prec):
+    s0, g, rng, sm, dr = _case(1, smoothing=0.2, drag=0.3)
+    prm = O.Params(dt=1e-3, drag=dr, smoothing=sm, exact=True)
+    T = 8
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    xT, g0, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, prec)
+    xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    tol = 1e-9 if prec == "fp64" else 2e-4
+    assert rel_err(xT, xw) < (1e-10 if prec == "fp64" else 1e-6)
+    for k, want in (("x", gw.x), ("v", gw.v), ("F", gw.F), ("C", gw.C), ("dFc", gw.Ft)):
+        e = norm_err(g0[k], want)
+        print(f"{prec} T={T} exact g{k} {e:.3e}")
+        assert e < tol, (k, e)
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_checkpointed_equals_full_tape(dm, prec):
+    s0, g, rng, _, _ = _case(2)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0, exact=True)
+    T = 12
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    x1, g1, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, prec, checkpoint_every=1)
+    x4, g4, cg4, _ = _rollout(dm, s0, g, prm, T, seed_gx, prec, checkpoint_every=5)
+    assert rel_err(x4, x1) < (1e-12 if prec == "fp64" else 1e-6)
+    for k in ("x", "v", "F", "C", "dFc"):
+        assert norm_err(g4[k], g1[k]) < (1e-10 if prec == "fp64" else 1e-4), k
+    with pytest.raises(Exception):
+        cg4.get_point_cloud(3).get("x")  # non-stored layer of a checkpointed graph
+
+
+def test_fp64_exact_gradient_matches_finite_differences(dm):
+    """Central differences (eps = 1e-4 scaled) along seeded directions."""
+    s0, g, rng, _, _ = _case(3, smoothing=0.1, drag=0.2)
+    prm = O.Params(dt=1e-3, drag=0.2, smoothing=0.1, exact=True)
+    T = 4
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    _, g0, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, "fp64")
+
+    def loss(s):
+        cg, keep = make_graph(dm, s, g, prm, precision="fp64", adjoint="exact", layers=T + 1)
+        cg.compute_forward_pass(0, 0)
+        return float((cg.get_point_cloud(T).get("x", np.float64) * seed_gx).sum())
+
+    for field, gkey, eps in (("v", "v", 1e-4), ("dFc", "dFc", 1e-5), ("x", "x", 1e-6)):
+        for _ in range(3):
+            d = rng.normal(size=getattr(s0, field).shape)
+            sp, sm_ = copy.deepcopy(s0), copy.deepcopy(s0)
+            setattr(sp, field, getattr(s0, field) + eps * d)
+            setattr(sm_, field, getattr(s0, field) - eps * d)
+            fd = (loss(sp) - loss(sm_)) / (2 * eps)
+            an = float((g0[gkey] * d).sum())
+            assert abs(an - fd) <= 1e-5 * abs(fd) + 1e-12, (field, an, fd)
+
+
+def test_tile_and_global_scatter_agree(dm):
+    s0, g, rng, _, _ = _case(4, G=16)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0, exact=True)
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    lib = dm._lib.lib
+    try:
+        lib.mpm_set_tile_nodes(0)
+        xa, ga, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")
+    finally:
+        lib.mpm_set_tile_nodes(2048)
+    xb, gb, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")
+    assert rel_err(xa, xb) < 1e-6
+    for k in ("x", "v", "F"):
+        assert norm_err(ga[k], gb[k]) < 1e-4, k
+
+
+@pytest.mark.parametrize("kernel,material", [("quadratic", "fcr"), ("cubic", "neohookean"), ("quadratic", "neohookean")])
+def test_optional_kernel_and_material(dm, orc, kernel, material):
+    s0, g, rng, _, _ = _case(5)
+    kid = {"cubic": 0, "quadratic": 1}[kernel]
+    mid = {"fcr": 0, "neohookean": 1}[material]
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.0, exact=True, kernel=kid, material=mid)
+    T = 4
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    xT, g0, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, "fp64", kernel=kernel, material=material)
+    xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    assert rel_err(xT, xw) < 1e-10
+    for k, want in (("x", gw.x), ("v", gw.v), ("dFc", gw.Ft)):
+        assert norm_err(g0[k], want) < 1e-9, k
+
+
+def test_particles_at_grid_boundary(dm, orc):
+    """Stencils that leave the grid: out-of-range nodes are skipped (reference
+    behaviour, ForwardSimulation.cpp:47-49); a ragged particle count."""
+    rng = np.random.default_rng(6)
+    n = 257
+    x = rng.uniform(0.0, 1.0, size=(n, 3))
+    x[:20] = rng.uniform(0.0, 0.03, size=(20, 3))
+    x[20:40] = rng.uniform(0.97, 1.0, size=(20, 3))
+    s0 = O.State(x, 0.3 * rng.normal(size=(n, 3)), 0.1 * rng.normal(size=(n, 3, 3)),
+                 np.eye(3) + 0.02 * rng.normal(size=(n, 3, 3)), np.full(n, 1e-3), np.full(n, 1e-4),
+                 np.full(n, 50.0), np.full(n, 30.0))
+    g = O.Grid((9, 9, 9), 1.0 / 8)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0, exact=False)
+    for prec in ("fp64", "fp32"):
+        cg, keep = make_graph(dm, s0, g, prm, precision=prec)
+        cg.compute_forward_pass(0, 0)
+        got = layer_state(cg, 1)
+        want, step = orc.forward_step(g, prm, s0)
+        assert rel_err(got["x"], want.x) < (1e-12 if prec == "fp64" else 1e-6)
+        assert rel_err(got["v"], want.v) < (1e-10 if prec == "fp64" else 1e-4)
+        g1 = O.Grads(rng.normal(size=(n, 3)), rng.normal(size=(n, 3)), rng.normal(size=(n, 3, 3)),
+                     rng.normal(size=(n, 3, 3)))
+        set_grads(cg, 1, g1)
+        cg.compute_backward_pass(0)
+        gb = orc.backward_step(g, prm, s0, want.C, step, g1)
+        assert norm_err(get_grads(cg, 0)["x"], gb.x) < (1e-9 if prec == "fp64" else 2e-3)
+
+
+def test_empty_point_cloud(dm):
+    pc = dm.PointCloud.create(0)
+    grid = dm.Grid(4, 4, 4, 0.25, (0, 0, 0))
+    cg = dm.CompGraph(pc, grid, grid)
+    cg.set_up_comp_graph(3)
+    cg.compute_forward_pass(0, 0)
+    cg.compute_backward_pass(0)
+    assert cg.get_point_cloud(2).get_positions().shape == (0, 3)
+    loss = cg.end_layer_mass_loss()
+    assert np.isfinite(loss)
+
+
+def test_compgraph_surface(dm, orc):
+    """CompGraph semantics of bind.cpp: layers, IndexError, render gradients,
+    optimisation steps, promotion."""
+    s0, g, rng, _, _ = _case(7, G=12)
+    prm = O.Params(dt=1e-3, drag=0.5, smoothing=0.1)
+    tgt = np.zeros(g.n_nodes)
+    orc.p2g_accumulate(g, s0.x + 0.02, s0.v, s0.C, s0.m, tgt, np.zeros((g.n_nodes, 3)))
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=5, target_mass=tgt)
+    assert cg.get_num_layers() == 5
+    with pytest.raises(IndexError):
+        cg.get_point_cloud(5)
+    with pytest.raises(IndexError):
+        cg.get_point_cloud_at_timestep(7)
+    cg.compute_forward_pass(0, 0)
+    l0 = cg.end_layer_mass_loss()
+    n = s0.n
+    assert not cg.has_render_gradients()
+    dF, dx = 1e-3 * rng.normal(size=(n, 3, 3)).astype(np.float32), 1e-3 * rng.normal(size=(n, 3)).astype(np.float32)
+    cg.set_render_gradients(dF, dx)
+    info = cg.get_render_gradient_info()
+    assert info["has_gradients"] and info["num_points"] == n
+    assert abs(info["grad_F_norm"] - np.linalg.norm(dF)) < 1e-4 * np.linalg.norm(dF)
+    cg.compute_backward_pass(0)
+    # render gradients were added to the last layer's loss gradient
+    last_gx = cg.get_grad(4, "x", np.float64)
+    _, d = orc.mass_loss(g, O.Params(), cg.get_point_cloud(4).get("x", np.float64), s0.m, tgt)
+    assert norm_err(last_gx, d["gx"] + dx) < 1e-4
+    with pytest.raises(RuntimeError, match="dLdF must be"):
+        cg.set_render_gradients(np.zeros((n, 3)), dx)
+    with pytest.raises(RuntimeError, match="Shape mismatch"):
+        cg.accumulate_render_grads(dF[:-1], dx[:-1])
+    cg.clear_render_gradients()
+    assert not cg.has_render_gradients()
+    # one optimisation step at layer 0 must not increase the loss
+    cg.optimize_single_timestep(0, max_gd_iters=1, initial_alpha=0.01, max_line_search_iters=6)
+    cg.compute_forward_pass(0, 0)
+    l1 = cg.end_layer_mass_loss()
+    assert l1 <= l0 + 1e-7
+    assert np.abs(cg.get_point_cloud(0).get_def_grads_morph()).max() > 0  # dFc moved
+    F_tot = cg.get_point_cloud(0).get_def_grads_total()
+    assert rel_err(F_tot, cg.get_point_cloud(0).get_def_grads() + cg.get_point_cloud(0).get_def_grads_morph()) < 1e-6
+    # invalid index: message and return, no raise (CompGraph.cpp:377-380)
+    cg.optimize_single_timestep(99)
+    x_last = cg.get_point_cloud(4).get_positions()
+    cg.promote_last_as_initial()
+    assert cg.get_num_layers() == 1
+    assert rel_err(cg.get_point_cloud(0).get_positions(), x_last) == 0.0
+
+
+def test_run_optimization_reduces_loss(dm, orc):
+    s0, g, rng, _, _ = _case(8, G=12)
+    tgt = np.zeros(g.n_nodes)
+    orc.p2g_accumulate(g, s0.x + np.array([0.03, 0.0, 0.0]), s0.v, s0.C, s0.m, tgt, np.zeros((g.n_nodes, 3)))
+    prm = O.Params(dt=1e-3, drag=0.5, smoothing=0.1)
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=1, target_mass=tgt)
+    opt = dm.OptInput()
+    opt.num_timesteps, opt.control_stride, opt.max_gd_iters, opt.max_ls_iters = 4, 2, 1, 4
+    opt.dt, opt.drag, opt.smoothing_factor, opt.initial_alpha, opt.gd_tol = 1e-3, 0.5, 0.1, 0.01, 1e-4
+    cg.set_up_comp_graph(4)
+    cg.set_sim_params(dt=1e-3, drag=0.5, smoothing=0.1)
+    cg.compute_forward_pass(0, 0)
+    before = cg.end_layer_mass_loss()
+    cg.run_optimization(opt)
+    cg.compute_forward_pass(0, 0)
+    after = cg.end_layer_mass_loss()
+    assert after <= before + 1e-7
+
+
+def test_autograd_rollout(dm):
+    torch = pytest.importorskip("torch")
+    from diffmpm_bindings.rollout import Rollout, mpm_rollout
+    from diffmpm_bindings import workloads as W
+    w = W.sphere32(seed=9, G=12, rho=60.0)
+    dev = torch.device("cuda")
+    sim = Rollout(w.n, w.dims, w.dx, steps=4, m=w.m[0], vol=w.vol[0], nu=0.3, dt=1e-3, precision="fp64",
+                  checkpoint_every=2)
+    x0 = torch.tensor(w.x, device=dev, requires_grad=True)
+    v0 = torch.tensor(w.v, device=dev, requires_grad=True)
+    F0 = torch.eye(3, dtype=torch.float64, device=dev).expand(w.n, 3, 3).contiguous().requires_grad_(True)
+    dFc = torch.zeros((w.n, 3, 3), dtype=torch.float64, device=dev, requires_grad=True)
+    E = torch.tensor(1e4, dtype=torch.float64, device=dev, requires_grad=True)
+    tgt = x0.detach() + 0.01
+    xT, FT = mpm_rollout(x0, v0, F0, dFc, E, sim)
+    loss = ((xT - tgt) ** 2).mean() + 0.1 * ((FT - torch.eye(3, dtype=torch.float64, device=dev)) ** 2).mean()
+    loss.backward()
+    for t in (x0, v0, F0, dFc):
+        assert t.grad is not None and torch.isfinite(t.grad).all()
+    # dL/dE against central differences of the same rollout
+    eps = 1.0
+
+    def L(Ev):
+        with torch.no_grad():
+            a, b = mpm_rollout(x0.detach(), v0.detach(), F0.detach(), dFc.detach(), torch.tensor(Ev, dtype=torch.float64, device=dev), sim)
+            return float((((a - tgt) ** 2).mean() + 0.1 * ((b - torch.eye(3, dtype=torch.float64, device=dev)) ** 2).mean()))
+    fd = (L(1e4 + eps) - L(1e4 - eps)) / (2 * eps)
+    assert abs(float(E.grad) - fd) <= 1e-4 * abs(fd) + 1e-14, (float(E.grad), fd)

@@ -3,10 +3,10 @@ the reference golden vectors.
 
 Tolerances: the plain FP64 engine must agree with the FP64 oracle to 1e-9
 relative (atomic summation order is the only difference).  The FP32 engine
-is held to the reference's own FP32 noise floor measured on the same inputs
-(tests/golden: float vs double build of the reference): x 1e-6, F 1e-5,
-v 2e-4 and C 3e-3 relative to the field's max magnitude, gradients 2e-3 in
-norm for one step.
+is held to tolerances below the reference's own FP32 noise floor on the same
+inputs (tests/golden: its float build differs from its double build by up to
+~1e-4 in C): x 1e-6, F 1e-6, v 2e-5 and C 1e-4 relative to the field's max
+magnitude, gradients 2e-3 in norm for one step.
 """
 import numpy as np
 import pytest
@@ -17,7 +17,7 @@ from helpers import (get_grads, golden_grid, golden_params, golden_state, layer_
 
 pytestmark = pytest.mark.gpu
 
-FWD_TOL = {"fp64": dict(x=1e-9, v=1e-9, C=1e-9, F=1e-9), "fp32": dict(x=1e-6, v=2e-4, C=3e-3, F=1e-5)}
+FWD_TOL = {"fp64": dict(x=1e-9, v=1e-9, C=1e-9, F=1e-9), "fp32": dict(x=1e-6, v=2e-5, C=1e-4, F=1e-6)}
 BWD_TOL = {"fp64": 1e-9, "fp32": 2e-3}
 
 
