@@ -112,6 +112,10 @@ void mpm_default_options(mpm_options* o);
 void mpm_set_verbose(int verbose);
 /* shared-memory node-tile budget of the scatter kernels (0 disables tiles) */
 int mpm_set_tile_nodes(int nodes);
+/* FP32 scatter strategy of P2G and the G2P transpose: 1 = segmented (one
+ * warp per run of particles sharing a cell, one lane per stencil node; the
+ * default), 0 = one thread per particle */
+int mpm_set_scatter_mode(int mode);
 /* CalculateLameParameters (Elasticity.cpp:149-153; bind.cpp:540-544) */
 int mpm_lame(double young, double poisson, double* lam, double* mu);
 

@@ -1053,6 +1053,14 @@ int mpm_set_tile_nodes(int nodes)
     });
 }
 
+int mpm_set_scatter_mode(int mode)
+{
+    return guard([&] {
+        if (mode != 0 && mode != 1) fail(MPM_ERR_ARG, "scatter mode must be 0 or 1");
+        g_scatter_mode = mode;
+    });
+}
+
 int mpm_lame(double E, double nu, double* lam, double* mu)
 {
     return guard([&] {

@@ -23,6 +23,7 @@
 namespace mpm {
 
 int g_tile_nodes = 2048;
+int g_scatter_mode = 1;
 
 namespace {
 
@@ -230,6 +231,205 @@ MPM_D void walk_rotated(const Stencil<R, K>& st, Fn&& f)
                 const R w = wab * sel(st.w[2], c), gc = sel(st.g[2], c);
                 f(st.base[0] + a, st.base[1] + b, st.base[2] + c, w, ga, gb, gc);
             }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// Segmented scatter (FP32).  Particles arrive sorted by cell, so runs of
+// particles share one stencil base.  Each block stages its chunk of
+// particles as records in shared memory and splits the chunk into segments
+// of equal base; a warp takes one segment at a time and each lane owns fixed
+// stencil nodes (lane and lane+32), summing the segment's contributions in
+// registers.  One shared atomic per node per segment replaces one per node
+// per particle, and no two lanes of a warp touch the same node.  The node
+// tile is then flushed to global memory once per block.  The contribution
+// of particle p to node n is  w_pn * [u0_p + A_p dg_pn, (m_p)].
+// ------------------------------------------------------------------------
+
+constexpr int kRec = 40;  // u0[3], m, A[9], pad[3], w[3][K<=4], g[3][K<=4]
+
+struct SegLayout {
+    float* rec;
+    int* sbase;
+    int* seg;
+    float* tile;
+};
+
+__device__ __forceinline__ SegLayout seg_layout(unsigned char* smem, int CH)
+{
+    SegLayout L;
+    L.rec = reinterpret_cast<float*>(smem);
+    L.sbase = reinterpret_cast<int*>(L.rec + (size_t)CH * kRec);
+    L.seg = L.sbase + 3 * CH;
+    L.tile = reinterpret_cast<float*>(L.seg + CH + 4);
+    return L;
+}
+
+inline size_t seg_smem_bytes(int CH, int tile_cap, int NC)
+{
+    return (size_t)CH * kRec * 4 + (size_t)(3 * CH + CH + 4) * 4 + (size_t)tile_cap * NC * 4;
+}
+
+template <int K, int NC>
+__device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const Stencil<float, K>& st,
+                            const float* u0, float m, const float* A, float* __restrict__ grid, int tile_cap,
+                            unsigned char* smem)
+{
+    const int CH = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = CH >> 5;
+    SegLayout L = seg_layout(smem, CH);
+    __shared__ int box[6];
+    __shared__ int wcnt[33];
+    // 1. records + bounding box of the chunk's stencil bases
+    if (t < 3) box[t] = INT_MAX;
+    else if (t < 6) box[t] = INT_MIN;
+    if (valid) {
+        float* r = L.rec + (size_t)t * kRec;
+        r[0] = u0[0];
+        r[1] = u0[1];
+        r[2] = u0[2];
+        r[3] = m;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) r[4 + i] = A[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int o = 0; o < K; ++o) {
+                r[16 + a * K + o] = st.w[a][o];
+                r[28 + a * K + o] = st.g[a][o];
+            }
+        L.sbase[t] = st.base[0];
+        L.sbase[CH + t] = st.base[1];
+        L.sbase[2 * CH + t] = st.base[2];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int lo = __reduce_min_sync(0xffffffffu, valid ? st.base[a] : INT_MAX);
+        int hi = __reduce_max_sync(0xffffffffu, valid ? st.base[a] : INT_MIN);
+        if (lane == 0) {
+            atomicMin(&box[a], lo);
+            atomicMax(&box[3 + a], hi);
+        }
+    }
+    // 2. segment starts: particles whose base differs from their predecessor
+    const bool f = valid && (t == 0 || L.sbase[t] != L.sbase[t - 1] || L.sbase[CH + t] != L.sbase[CH + t - 1] ||
+                             L.sbase[2 * CH + t] != L.sbase[2 * CH + t - 1]);
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wcnt[warp] = __popc(bal);
+    __syncthreads();
+    if (t == 0) {
+        int acc = 0;
+        for (int w = 0; w < nw; ++w) {
+            const int c = wcnt[w];
+            wcnt[w] = acc;
+            acc += c;
+        }
+        wcnt[32] = acc;
+    }
+    __syncthreads();
+    const int nseg = wcnt[32];
+    if (f) L.seg[wcnt[warp] + __popc(bal & ((1u << lane) - 1u))] = t;
+    if (t == 0) L.seg[nseg] = nvalid;
+    // 3. node tile over the bounding box, if it fits
+    bool tile = false;
+    int b0 = 0, b1 = 0, b2 = 0, e1 = 0, e2 = 0, vol = 0;
+    if (tile_cap > 0 && box[0] != INT_MAX) {
+        const long long x0 = (long long)box[3] - box[0] + K, x1 = (long long)box[4] - box[1] + K,
+                        x2 = (long long)box[5] - box[2] + K;
+        if (x0 > 0 && x1 > 0 && x2 > 0 && x0 <= tile_cap && x1 <= tile_cap && x2 <= tile_cap &&
+            x0 * x1 * x2 <= tile_cap) {
+            tile = true;
+            b0 = box[0];
+            b1 = box[1];
+            b2 = box[2];
+            e1 = (int)x1;
+            e2 = (int)x2;
+            vol = (int)(x0 * x1 * x2);
+            for (int i = t; i < NC * vol; i += CH) L.tile[i] = 0.f;
+        }
+    }
+    __syncthreads();
+    // 4. warps over segments, lanes over nodes
+    constexpr int NODES = K * K * K;
+    const int n0 = lane, n1 = lane + 32;
+    const int a0 = n0 / (K * K), bb = (n0 / K) % K, cc = n0 % K;
+    const bool has1 = n1 < NODES;
+    const int a1 = has1 ? n1 / (K * K) : 0;
+    for (int sg = warp; sg < nseg; sg += nw) {
+        const int p0 = L.seg[sg], p1 = L.seg[sg + 1];
+        float acc0[NC], acc1[NC];
+#pragma unroll
+        for (int q = 0; q < NC; ++q) acc0[q] = acc1[q] = 0.f;
+        if (n0 < NODES) {
+            for (int p = p0; p < p1; ++p) {
+                const float* r = L.rec + (size_t)p * kRec;
+                const float4 q0 = *reinterpret_cast<const float4*>(r);
+                const float4 qa = *reinterpret_cast<const float4*>(r + 4);
+                const float4 qb = *reinterpret_cast<const float4*>(r + 8);
+                const float a8 = r[12];
+                const float wy = r[16 + K + bb], wz = r[16 + 2 * K + cc];
+                const float gy = r[28 + K + bb], gz = r[28 + 2 * K + cc];
+                const float wyz = wy * wz;
+                // A row-major: (qa.x qa.y qa.z | qa.w qb.x qb.y | qb.z qb.w a8)
+                const float c0 = q0.x + qa.y * gy + qa.z * gz;
+                const float c1 = q0.y + qb.x * gy + qb.y * gz;
+                const float c2 = q0.z + qb.w * gy + a8 * gz;
+                {
+                    const float w = r[16 + a0] * wyz, gx = r[28 + a0];
+                    acc0[0] += w * (c0 + qa.x * gx);
+                    acc0[1] += w * (c1 + qa.w * gx);
+                    acc0[2] += w * (c2 + qb.z * gx);
+                    if (NC == 4) acc0[NC - 1] += w * q0.w;
+                }
+                if (has1) {
+                    const float w = r[16 + a1] * wyz, gx = r[28 + a1];
+                    acc1[0] += w * (c0 + qa.x * gx);
+                    acc1[1] += w * (c1 + qa.w * gx);
+                    acc1[2] += w * (c2 + qb.z * gx);
+                    if (NC == 4) acc1[NC - 1] += w * q0.w;
+                }
+            }
+            const int i0 = L.sbase[p0], j0 = L.sbase[CH + p0], k0 = L.sbase[2 * CH + p0];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (h == 1 && !has1) break;
+                const float* acc = h == 0 ? acc0 : acc1;
+                const int i = i0 + (h == 0 ? a0 : a1), j = j0 + bb, k = k0 + cc;
+                if (tile) {
+                    const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q)
+                        if (acc[q] != 0.f) atomicAdd(&L.tile[q * vol + idx], acc[q]);
+                } else if (in_grid(kp, i, j, k)) {
+                    const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+                    for (int q = 0; q < NC; ++q)
+                        if (acc[q] != 0.f) atomicAdd(&grid[nd * 4 + q], acc[q]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // 5. flush the tile
+    if (tile) {
+        for (int u = t; u < vol; u += CH) {
+            float v[NC];
+            bool any = false;
+#pragma unroll
+            for (int q = 0; q < NC; ++q) {
+                v[q] = L.tile[q * vol + u];
+                any |= v[q] != 0.f;
+            }
+            if (!any) continue;
+            const int kk = u % e2, rr = u / e2;
+            const int jj = rr % e1, ii = rr / e1;
+            const int i = b0 + ii, j = b1 + jj, k = b2 + kk;
+            if (!in_grid(kp, i, j, k)) continue;
+            const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+            for (int q = 0; q < NC; ++q)
+                if (v[q] != 0.f) atomicAdd(&grid[nd * 4 + q], v[q]);
         }
     }
 }
@@ -540,6 +740,71 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj(KP<R> kp, int n, long long
         });
     }
     sc.flush(kp, adj);
+}
+
+// P_op_1 + P2G with the segmented scatter (FP32 path)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_p2g_seg(KP<float> kp, int n, long long ld, const float* __restrict__ st,
+                                                       const float* __restrict__ dfc, const float* __restrict__ co,
+                                                       float* __restrict__ grid, int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    const int nvalid = min((int)blockDim.x, n - (int)(blockIdx.x * blockDim.x));
+    Stencil<float, K> sten;
+    float A[9], mv[3], mass = 0.f;
+    if (valid) {
+        float x[3], v[3], C[9], F[9], Ft[9];
+        load_planes(st + ST_X * ld, ld, p, 3, x);
+        load_planes(st + ST_V * ld, ld, p, 3, v);
+        load_planes(st + ST_C * ld, ld, p, 9, C);
+        load_Ft(st, dfc, ld, p, F, Ft);
+        mass = co[CO_M * ld + p];
+        const float vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
+        Inv<float> iv;
+        invariants(Ft, iv);
+        float P[9], Rm[9], S[9], PF[9];
+        pk(kp.material, Ft, lam, mu, iv, P, Rm, S);
+        mulNT3(P, Ft, PF);
+        const float trC = C[0] + C[4] + C[8];
+        const float k1 = -kp.C0 * kp.dt * vol;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = k1 * (PF[i] + ((i % 4 == 0) ? kp.bulk * trC : 0.f)) + mass * C[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) mv[a] = mass * v[a] * kp.dragf;
+        make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    seg_scatter<K, 4>(kp, nvalid, valid, sten, mv, mass, A, grid, tile_cap, smem);
+}
+
+// P_op_2^T + G2P^T with the segmented scatter (FP32 path)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_g2p_adj_seg(KP<float> kp, int n, long long ld,
+                                                           const float* __restrict__ st, const float* __restrict__ dfc,
+                                                           const float* __restrict__ st1, const float* __restrict__ g1,
+                                                           const float* __restrict__ trust, float* __restrict__ adj,
+                                                           int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    const int nvalid = min((int)blockDim.x, n - (int)(blockIdx.x * blockDim.x));
+    Stencil<float, K> sten;
+    float vb[3], CC[9];
+    if (valid) {
+        float x[3], F[9], Ft[9];
+        load_planes(st + ST_X * ld, ld, p, 3, x);
+        load_Ft(st, dfc, ld, p, F, Ft);
+        PostAdj<float> o;
+        post_adjoint(kp, ld, p, Ft, st1, g1, trust, o);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) vb[a] = o.vbar[a];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) CC[i] = kp.C0 * o.Cbar[i];
+        make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    seg_scatter<K, 3>(kp, nvalid, valid, sten, vb, 0.f, CC, adj, tile_cap, smem);
 }
 
 // G_op^T (BackPropagation.cpp:59-72)
@@ -1033,8 +1298,21 @@ void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
 {
     if (n <= 0) return;
     const int cap = tile_cap_for<R>();
-    const size_t sm = (size_t)cap * 4 * sizeof(R);
     auto kp = make_kp<R>(c);
+    if constexpr (sizeof(R) == 4) {
+        if (g_scatter_mode == 1) {
+            const size_t sm = seg_smem_bytes(kThreads, cap, 4);
+            if (c.kernel == 0) {
+                cudaFuncSetAttribute(k_p2g_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                k_p2g_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+            } else {
+                cudaFuncSetAttribute(k_p2g_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                k_p2g_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+            }
+            return;
+        }
+    }
+    const size_t sm = (size_t)cap * 4 * sizeof(R);
     if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
     else k_p2g<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
 }
@@ -1062,8 +1340,21 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
 {
     if (n <= 0) return;
     const int cap = tile_cap_for<R>();
-    const size_t sm = (size_t)cap * 3 * sizeof(R);
     auto kp = make_kp<R>(c);
+    if constexpr (sizeof(R) == 4) {
+        if (g_scatter_mode == 1) {
+            const size_t sm = seg_smem_bytes(kThreads, cap, 3);
+            if (c.kernel == 0) {
+                cudaFuncSetAttribute(k_g2p_adj_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                k_g2p_adj_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+            } else {
+                cudaFuncSetAttribute(k_g2p_adj_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                k_g2p_adj_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+            }
+            return;
+        }
+    }
+    const size_t sm = (size_t)cap * 3 * sizeof(R);
     if (c.kernel == 0) k_g2p_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
     else k_g2p_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
 }

@@ -32,6 +32,9 @@ struct StepCfg {
 
 // Shared-memory tile budget (nodes) for the scatter kernels; 0 disables tiles.
 extern int g_tile_nodes;
+// FP32 scatter strategy: 1 = segmented (warp per cell segment, lane per
+// node), 0 = per-particle scatter
+extern int g_scatter_mode;
 
 template <typename R>
 void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,

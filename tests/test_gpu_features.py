@@ -96,20 +96,39 @@ def test_fp64_exact_gradient_matches_finite_differences(dm):
             assert abs(an - fd) <= 1e-5 * abs(fd) + 1e-12, (field, an, fd)
 
 
-def test_tile_and_global_scatter_agree(dm):
+@pytest.mark.parametrize("mode,tile", [(0, 0), (0, 2048), (1, 0), (1, 64)])
+def test_scatter_strategies_agree(dm, mode, tile):
+    """Segmented vs per-particle scatter, with and without the shared node
+    tile (tile 64 forces the global-atomic fallback for most blocks)."""
     s0, g, rng, _, _ = _case(4, G=16)
     prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0, exact=True)
     seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
     lib = dm._lib.lib
+    xb, gb, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")  # defaults: segmented + tile 2048
     try:
-        lib.mpm_set_tile_nodes(0)
+        lib.mpm_set_scatter_mode(mode)
+        lib.mpm_set_tile_nodes(tile)
         xa, ga, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")
     finally:
+        lib.mpm_set_scatter_mode(1)
         lib.mpm_set_tile_nodes(2048)
-    xb, gb, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")
     assert rel_err(xa, xb) < 1e-6
     for k in ("x", "v", "F"):
         assert norm_err(ga[k], gb[k]) < 1e-4, k
+
+
+def test_unsorted_particles(dm, orc):
+    """Shuffled particle order (segments of length one) gives the same step."""
+    s0, g, rng, _, _ = _case(10, G=12)
+    perm = rng.permutation(s0.n)
+    sp = O.State(s0.x[perm], s0.v[perm], s0.C[perm], s0.F[perm], s0.m[perm], s0.vol[perm], s0.lam[perm],
+                 s0.mu[perm], s0.dFc[perm])
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
+    cg, keep = make_graph(dm, sp, g, prm, precision="fp32")
+    cg.compute_forward_pass(0, 0)
+    want, _ = orc.forward_step(g, prm, sp)
+    got = layer_state(cg, 1)
+    assert rel_err(got["x"], want.x) < 1e-6 and rel_err(got["C"], want.C) < 1e-4
 
 
 @pytest.mark.parametrize("kernel,material", [("quadratic", "fcr"), ("cubic", "neohookean"), ("quadratic", "neohookean")])
