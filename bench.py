@@ -50,7 +50,7 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def make_workload(name: str, quick: bool = False):
+def make_workload(name: str, quick: bool = False, timesteps: int = 0):
     from diffmpm_bindings import workloads as W
     if name == "spheres2m":
         w = W.spheres2m(n=200_000 if quick else 2_000_000, steps=40 if quick else 400, checkpoint=20)
@@ -61,6 +61,8 @@ def make_workload(name: str, quick: bool = False):
         w.checkpoint = 1
     else:
         raise SystemExit(f"unknown workload {name}")
+    if timesteps:
+        w.steps = timesteps
     if w.target is None:
         rng = np.random.default_rng(11)
         w.target = w.x + 0.02 * np.sin(2 * np.pi * w.x[:, [1, 2, 0]] + rng.random(3))
@@ -162,7 +164,7 @@ def run_ours(args, rank, world, device):
     import diffmpm_bindings as dm
     lib = dm._lib.lib
     lib.mpm_set_verbose(0)
-    w = make_workload(args.workload, args.quick)
+    w = make_workload(args.workload, args.quick, args.timesteps)
     n, T = w.n, w.steps
     cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
     cg.set_up_comp_graph(T + 1)
@@ -227,7 +229,7 @@ def run_ours(args, rank, world, device):
             "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][1])}}
 
     # ---- e2e through the public API with host buffers
-    e2e = run_e2e(torch, dm, args, w, device, keep)
+    e2e = None if args.no_e2e else run_e2e(torch, dm, args, w, device, keep)
 
     # ---- plain FP64 form and accuracy (rank 0)
     fp64 = None
@@ -376,7 +378,7 @@ def cpu_baseline(w, args):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    w = make_workload(args.workload, args.quick)
+    w = make_workload(args.workload, args.quick, args.timesteps)
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
@@ -424,6 +426,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="reduced workload for smoke runs")
+    ap.add_argument("--timesteps", type=int, default=0, help="override the workload's timestep count")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

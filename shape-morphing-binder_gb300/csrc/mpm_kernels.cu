@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstdint>
+#include <unordered_map>
 
 #include "mpm_launch.h"
 #include "mpm_math.cuh"
@@ -249,42 +250,24 @@ MPM_D void walk_rotated(const Stencil<R, K>& st, Fn&& f)
 
 constexpr int kRec = 40;  // u0[3], m, A[9], pad[3], w[3][K<=4], g[3][K<=4]
 
-struct SegLayout {
-    float* rec;
-    int* sbase;
-    int* seg;
-    float* tile;
-};
-
-__device__ __forceinline__ SegLayout seg_layout(unsigned char* smem, int CH)
-{
-    SegLayout L;
-    L.rec = reinterpret_cast<float*>(smem);
-    L.sbase = reinterpret_cast<int*>(L.rec + (size_t)CH * kRec);
-    L.seg = L.sbase + 3 * CH;
-    L.tile = reinterpret_cast<float*>(L.seg + CH + 4);
-    return L;
-}
-
 inline size_t seg_smem_bytes(int CH, int tile_cap, int NC)
 {
-    return (size_t)CH * kRec * 4 + (size_t)(3 * CH + CH + 4) * 4 + (size_t)tile_cap * NC * 4;
+    return (size_t)CH * kRec * 4 + (size_t)tile_cap * NC * 4;
 }
 
 template <int K, int NC>
-__device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const Stencil<float, K>& st,
-                            const float* u0, float m, const float* A, float* __restrict__ grid, int tile_cap,
-                            unsigned char* smem)
+__device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float, K>& st, const float* u0, float m,
+                            const float* A, float* __restrict__ grid, int tile_cap, unsigned char* smem)
 {
-    const int CH = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5, nw = CH >> 5;
-    SegLayout L = seg_layout(smem, CH);
+    const int CH = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    float* recs = reinterpret_cast<float*>(smem);
+    float* tilebuf = recs + (size_t)CH * kRec;
     __shared__ int box[6];
-    __shared__ int wcnt[33];
-    // 1. records + bounding box of the chunk's stencil bases
+    // 1. this lane's record, the block's bounding box of stencil bases
     if (t < 3) box[t] = INT_MAX;
     else if (t < 6) box[t] = INT_MIN;
     if (valid) {
-        float* r = L.rec + (size_t)t * kRec;
+        float* r = recs + (size_t)t * kRec;
         r[0] = u0[0];
         r[1] = u0[1];
         r[2] = u0[2];
@@ -298,39 +281,26 @@ __device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const S
                 r[16 + a * K + o] = st.w[a][o];
                 r[28 + a * K + o] = st.g[a][o];
             }
-        L.sbase[t] = st.base[0];
-        L.sbase[CH + t] = st.base[1];
-        L.sbase[2 * CH + t] = st.base[2];
     }
     __syncthreads();
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        int lo = __reduce_min_sync(0xffffffffu, valid ? st.base[a] : INT_MAX);
-        int hi = __reduce_max_sync(0xffffffffu, valid ? st.base[a] : INT_MIN);
+        const int lo = __reduce_min_sync(0xffffffffu, valid ? st.base[a] : INT_MAX);
+        const int hi = __reduce_max_sync(0xffffffffu, valid ? st.base[a] : INT_MIN);
         if (lane == 0) {
             atomicMin(&box[a], lo);
             atomicMax(&box[3 + a], hi);
         }
     }
-    // 2. segment starts: particles whose base differs from their predecessor
-    const bool f = valid && (t == 0 || L.sbase[t] != L.sbase[t - 1] || L.sbase[CH + t] != L.sbase[CH + t - 1] ||
-                             L.sbase[2 * CH + t] != L.sbase[2 * CH + t - 1]);
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) wcnt[warp] = __popc(bal);
+    // 2. groups of lanes sharing a stencil base (not necessarily contiguous:
+    //    particles drift across cells between sorts)
+    const unsigned long long key =
+        valid ? (((unsigned long long)(st.base[0] & 0x1FFFFF) << 42) |
+                 ((unsigned long long)(st.base[1] & 0x1FFFFF) << 21) | (unsigned long long)(st.base[2] & 0x1FFFFF))
+              : ~0ull;
+    const unsigned grp = __match_any_sync(0xffffffffu, key);
+    unsigned todo = __ballot_sync(0xffffffffu, valid);
     __syncthreads();
-    if (t == 0) {
-        int acc = 0;
-        for (int w = 0; w < nw; ++w) {
-            const int c = wcnt[w];
-            wcnt[w] = acc;
-            acc += c;
-        }
-        wcnt[32] = acc;
-    }
-    __syncthreads();
-    const int nseg = wcnt[32];
-    if (f) L.seg[wcnt[warp] + __popc(bal & ((1u << lane) - 1u))] = t;
-    if (t == 0) L.seg[nseg] = nvalid;
     // 3. node tile over the bounding box, if it fits
     bool tile = false;
     int b0 = 0, b1 = 0, b2 = 0, e1 = 0, e2 = 0, vol = 0;
@@ -346,31 +316,39 @@ __device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const S
             e1 = (int)x1;
             e2 = (int)x2;
             vol = (int)(x0 * x1 * x2);
-            for (int i = t; i < NC * vol; i += CH) L.tile[i] = 0.f;
+            for (int i = t; i < NC * vol; i += CH) tilebuf[i] = 0.f;
         }
     }
     __syncthreads();
-    // 4. warps over segments, lanes over nodes
+    // 4. each warp walks its runs; lane owns stencil nodes lane and lane+32
     constexpr int NODES = K * K * K;
     const int n0 = lane, n1 = lane + 32;
     const int a0 = n0 / (K * K), bb = (n0 / K) % K, cc = n0 % K;
-    const bool has1 = n1 < NODES;
+    const bool has0 = n0 < NODES, has1 = n1 < NODES;
     const int a1 = has1 ? n1 / (K * K) : 0;
-    for (int sg = warp; sg < nseg; sg += nw) {
-        const int p0 = L.seg[sg], p1 = L.seg[sg + 1];
+    const float* wrec = recs + (size_t)(warp * 32) * kRec;
+    while (todo) {
+        const int lead = __ffs(todo) - 1;
+        const unsigned members = __shfl_sync(0xffffffffu, grp, lead);
+        todo &= ~members;
+        const int i0 = __shfl_sync(0xffffffffu, st.base[0], lead);
+        const int j0 = __shfl_sync(0xffffffffu, st.base[1], lead);
+        const int k0 = __shfl_sync(0xffffffffu, st.base[2], lead);
         float acc0[NC], acc1[NC];
 #pragma unroll
         for (int q = 0; q < NC; ++q) acc0[q] = acc1[q] = 0.f;
-        if (n0 < NODES) {
-            for (int p = p0; p < p1; ++p) {
-                const float* r = L.rec + (size_t)p * kRec;
+        if (has0) {
+            unsigned mm = members;
+            while (mm) {
+                const int p = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const float* r = wrec + (size_t)p * kRec;
                 const float4 q0 = *reinterpret_cast<const float4*>(r);
                 const float4 qa = *reinterpret_cast<const float4*>(r + 4);
                 const float4 qb = *reinterpret_cast<const float4*>(r + 8);
                 const float a8 = r[12];
-                const float wy = r[16 + K + bb], wz = r[16 + 2 * K + cc];
+                const float wyz = r[16 + K + bb] * r[16 + 2 * K + cc];
                 const float gy = r[28 + K + bb], gz = r[28 + 2 * K + cc];
-                const float wyz = wy * wz;
                 // A row-major: (qa.x qa.y qa.z | qa.w qb.x qb.y | qb.z qb.w a8)
                 const float c0 = q0.x + qa.y * gy + qa.z * gz;
                 const float c1 = q0.y + qb.x * gy + qb.y * gz;
@@ -390,7 +368,6 @@ __device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const S
                     if (NC == 4) acc1[NC - 1] += w * q0.w;
                 }
             }
-            const int i0 = L.sbase[p0], j0 = L.sbase[CH + p0], k0 = L.sbase[2 * CH + p0];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 if (h == 1 && !has1) break;
@@ -400,7 +377,7 @@ __device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const S
                     const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
 #pragma unroll
                     for (int q = 0; q < NC; ++q)
-                        if (acc[q] != 0.f) atomicAdd(&L.tile[q * vol + idx], acc[q]);
+                        if (acc[q] != 0.f) atomicAdd(&tilebuf[q * vol + idx], acc[q]);
                 } else if (in_grid(kp, i, j, k)) {
                     const long long nd = node_of(kp, i, j, k);
 #pragma unroll
@@ -418,7 +395,7 @@ __device__ void seg_scatter(const KP<float>& kp, int nvalid, bool valid, const S
             bool any = false;
 #pragma unroll
             for (int q = 0; q < NC; ++q) {
-                v[q] = L.tile[q * vol + u];
+                v[q] = tilebuf[q * vol + u];
                 any |= v[q] != 0.f;
             }
             if (!any) continue;
@@ -544,7 +521,116 @@ MPM_D void load_node4<double>(const double* __restrict__ grid, long long nd, dou
     v[3] = b.y;
 }
 
+// ------------------------------------------------------------------------
+// Gather tile (FP32): the block's stencil bounding box of one or two node
+// arrays (float4 per node) is copied into shared memory once, so the 64
+// per-particle node reads hit shared memory instead of L1/L2.  Blocks whose
+// box exceeds the budget read global memory directly.
+// ------------------------------------------------------------------------
+struct GTile {
+    bool on;
+    int b0, b1, b2, e1, e2;
+    __device__ __forceinline__ int index(int i, int j, int k) const { return ((i - b0) * e1 + (j - b1)) * e2 + (k - b2); }
+};
+
+template <int K, int NA>
+__device__ GTile stage_gather_tile(const KP<float>& kp, bool valid, const int* base, const float4* __restrict__ s0,
+                                   const float4* __restrict__ s1, float4* d0, float4* d1, int cap)
+{
+    __shared__ int box[6];
+    const int t = threadIdx.x, lane = t & 31;
+    if (t < 3) box[t] = INT_MAX;
+    else if (t < 6) box[t] = INT_MIN;
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int lo = __reduce_min_sync(0xffffffffu, valid ? base[a] : INT_MAX);
+        const int hi = __reduce_max_sync(0xffffffffu, valid ? base[a] : INT_MIN);
+        if (lane == 0) {
+            atomicMin(&box[a], lo);
+            atomicMax(&box[3 + a], hi);
+        }
+    }
+    __syncthreads();
+    GTile g;
+    g.on = false;
+    g.b0 = g.b1 = g.b2 = g.e1 = g.e2 = 0;
+    if (cap > 0 && box[0] != INT_MAX) {
+        const long long x0 = (long long)box[3] - box[0] + K, x1 = (long long)box[4] - box[1] + K,
+                        x2 = (long long)box[5] - box[2] + K;
+        if (x0 > 0 && x1 > 0 && x2 > 0 && x0 <= cap && x1 <= cap && x2 <= cap && x0 * x1 * x2 <= cap) {
+            g.on = true;
+            g.b0 = box[0];
+            g.b1 = box[1];
+            g.b2 = box[2];
+            g.e1 = (int)x1;
+            g.e2 = (int)x2;
+            const int vol = (int)(x0 * x1 * x2);
+            for (int u = t; u < vol; u += blockDim.x) {
+                const int kk = u % g.e2, rr = u / g.e2;
+                const int jj = rr % g.e1, ii = rr / g.e1;
+                const int i = g.b0 + ii, j = g.b1 + jj, k = g.b2 + kk;
+                float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+                if (in_grid(kp, i, j, k)) {
+                    const long long nd = node_of(kp, i, j, k);
+                    v0 = __ldg(s0 + nd);
+                    if (NA == 2) v1 = __ldg(s1 + nd);
+                }
+                d0[u] = v0;
+                if (NA == 2) d1[u] = v1;
+            }
+        }
+    }
+    __syncthreads();
+    return g;
+}
+
 // ------------------------------------------------------------------ G2P
+
+// G2P epilogue (ForwardSimulation.cpp:120-157): C from the gathered moments,
+// J trust region, F update with smoothing, advection, stores of layer n+1.
+template <typename R>
+MPM_D void g2p_finish(const KP<R>& kp, long long ld, int p, const R* x, const R* F, const R* Ft, const R* vs,
+                      const R* Cx, const R* Cy, const R* Cz, R* __restrict__ st1, R* __restrict__ trust)
+{
+    R Cn[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        Cn[r * 3 + 0] = kp.C0 * Cx[r];
+        Cn[r * 3 + 1] = kp.C0 * Cy[r];
+        Cn[r * 3 + 2] = kp.C0 * Cz[r];
+    }
+    // J trust region (ForwardSimulation.cpp:135-152)
+    R s_tr = R(1);
+    if (kp.jmin > R(0)) {
+        R J0 = R(1) + det_minus_one(Ft);
+        J0 = J0 > R(1e-6) ? J0 : R(1e-6);
+        const R trC = Cn[0] + Cn[4] + Cn[8];
+        if (trC < R(0)) {
+            const R denom = kp.dt * trC;
+            const R s = (kp.jmin / J0 - R(1)) / (denom < R(-1e-6) ? denom : R(-1e-6));
+            if (s < R(1)) {
+                s_tr = s < R(0) ? R(0) : s;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Cn[i] *= s_tr;
+            }
+        }
+    }
+    R IdtC[9], Fn[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IdtC[i] = ((i % 4 == 0) ? R(1) : R(0)) + kp.dt * Cn[i];
+    mul3(IdtC, Ft, Fn);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Fn[i] = Fn[i] * (R(1) - kp.s) + F[i] * kp.s;
+    R x1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x1[a] = x[a] + kp.dt * vs[a];
+    store_planes(st1 + ST_X * ld, ld, p, 3, x1);
+    store_planes(st1 + ST_V * ld, ld, p, 3, vs);
+    store_planes(st1 + ST_C * ld, ld, p, 9, Cn);
+    store_planes(st1 + ST_F * ld, ld, p, 9, Fn);
+    if (trust) trust[p] = s_tr;
+}
 
 template <typename R, int K>
 __global__ void __launch_bounds__(kThreads) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
@@ -601,43 +687,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KP<R> kp, int n, long long ld,
             Cz[r] += wx * t2[r];
         }
     }
-    R Cn[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        Cn[r * 3 + 0] = kp.C0 * Cx[r];
-        Cn[r * 3 + 1] = kp.C0 * Cy[r];
-        Cn[r * 3 + 2] = kp.C0 * Cz[r];
-    }
-    // J trust region (ForwardSimulation.cpp:135-152)
-    R s_tr = R(1);
-    if (kp.jmin > R(0)) {
-        R J0 = R(1) + det_minus_one(Ft);
-        J0 = J0 > R(1e-6) ? J0 : R(1e-6);
-        const R trC = Cn[0] + Cn[4] + Cn[8];
-        if (trC < R(0)) {
-            const R denom = kp.dt * trC;
-            const R s = (kp.jmin / J0 - R(1)) / (denom < R(-1e-6) ? denom : R(-1e-6));
-            if (s < R(1)) {
-                s_tr = s < R(0) ? R(0) : s;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) Cn[i] *= s_tr;
-            }
-        }
-    }
-    R IdtC[9], Fn[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) IdtC[i] = ((i % 4 == 0) ? R(1) : R(0)) + kp.dt * Cn[i];
-    mul3(IdtC, Ft, Fn);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) Fn[i] = Fn[i] * (R(1) - kp.s) + F[i] * kp.s;
-    R x1[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) x1[a] = x[a] + kp.dt * vs[a];
-    store_planes(st1 + ST_X * ld, ld, p, 3, x1);
-    store_planes(st1 + ST_V * ld, ld, p, 3, vs);
-    store_planes(st1 + ST_C * ld, ld, p, 9, Cn);
-    store_planes(st1 + ST_F * ld, ld, p, 9, Fn);
-    if (trust) trust[p] = s_tr;
+    g2p_finish(kp, ld, p, x, F, Ft, vs, Cx, Cy, Cz, st1, trust);
 }
 
 // ------------------------------------------------------------- adjoint
@@ -751,7 +801,6 @@ __global__ void __launch_bounds__(kThreads) k_p2g_seg(KP<float> kp, int n, long 
     extern __shared__ __align__(16) unsigned char smem[];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
-    const int nvalid = min((int)blockDim.x, n - (int)(blockIdx.x * blockDim.x));
     Stencil<float, K> sten;
     float A[9], mv[3], mass = 0.f;
     if (valid) {
@@ -775,7 +824,7 @@ __global__ void __launch_bounds__(kThreads) k_p2g_seg(KP<float> kp, int n, long 
         for (int a = 0; a < 3; ++a) mv[a] = mass * v[a] * kp.dragf;
         make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
     }
-    seg_scatter<K, 4>(kp, nvalid, valid, sten, mv, mass, A, grid, tile_cap, smem);
+    seg_scatter<K, 4>(kp, valid, sten, mv, mass, A, grid, tile_cap, smem);
 }
 
 // P_op_2^T + G2P^T with the segmented scatter (FP32 path)
@@ -789,7 +838,6 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj_seg(KP<float> kp, int n, l
     extern __shared__ __align__(16) unsigned char smem[];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
-    const int nvalid = min((int)blockDim.x, n - (int)(blockIdx.x * blockDim.x));
     Stencil<float, K> sten;
     float vb[3], CC[9];
     if (valid) {
@@ -804,7 +852,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj_seg(KP<float> kp, int n, l
         for (int i = 0; i < 9; ++i) CC[i] = kp.C0 * o.Cbar[i];
         make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
     }
-    seg_scatter<K, 3>(kp, nvalid, valid, sten, vb, 0.f, CC, adj, tile_cap, smem);
+    seg_scatter<K, 3>(kp, valid, sten, vb, 0.f, CC, adj, tile_cap, smem);
 }
 
 // G_op^T (BackPropagation.cpp:59-72)
@@ -842,10 +890,14 @@ __global__ void __launch_bounds__(kThreads) k_p2g_adj(KP<R> kp, int n, long long
                                                        const R* __restrict__ trust, const R* __restrict__ grid,
                                                        const R* __restrict__ adj, R* __restrict__ g,
                                                        R* __restrict__ gFt_out, R* __restrict__ glam,
-                                                       R* __restrict__ gmu)
+                                                       R* __restrict__ gmu, int cap)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    // tail threads of the last block mirror particle n-1 (never stored) so the
+    // whole block can take part in staging the node tile
+    const int p_raw = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p_raw < n;
+    const int p = valid ? p_raw : n - 1;
     R x[3], v[3], C[9], F[9], Ft[9];
     load_planes(st + ST_X * ld, ld, p, 3, x);
     load_planes(st + ST_V * ld, ld, p, 3, v);
@@ -873,54 +925,119 @@ __global__ void __launch_bounds__(kThreads) k_p2g_adj(KP<R> kp, int n, long long
 
     Stencil<R, K> sn;
     make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, true);
+    GTile tl;
+    tl.on = false;
+    tl.b0 = tl.b1 = tl.b2 = tl.e1 = tl.e2 = 0;
+    float4* ta = reinterpret_cast<float4*>(smem);
+    float4* tg = ta + (cap > 0 ? cap : 0);
+    if constexpr (sizeof(R) == 4) {
+        tl = stage_gather_tile<K, 2>(kp, true, sn.base, reinterpret_cast<const float4*>(adj),
+                                     reinterpret_cast<const float4*>(grid), ta, tg, cap);
+    }
+    // Separable accumulation over the K^3 stencil.  Per node n = (a,b,c) with
+    // d = (dL/dp, dL/dm) and v_i the node velocity:
+    //   sig_n = m dL/dm + (m v' + A dg).dL/dp + v_i.(vbar + C0 Cbar dg)
+    //   ax += sig_n grad w_n,  bp += w_n dL/dp,  bv += w_n v_i,
+    //   M1 += w_n dL/dp dg^T
+    // with w_n = wx_a wy_b wz_c and grad w_n = -(1/dx)(sx wy wz, wx sy wz,
+    // wx wy sz); the sums over c, then b, are folded into per-(a,b) and
+    // per-a partials so each node costs ~24 FMAs.
     R M1[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ax[3] = {0, 0, 0}, bp[3] = {0, 0, 0}, bv[3] = {0, 0, 0};
-    const R nidx = -kp.inv_dx;
 #pragma unroll
     for (int a = 0; a < K; ++a) {
         const int i = sn.base[0] + a;
         if ((unsigned)i >= (unsigned)kp.dims[0]) continue;
+        const R gxa = sn.g[0][a];
+        R Pa[3], Qa[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            Pa[r] = mvv[r] + A[r * 3] * gxa;
+            Qa[r] = o.vbar[r] + CC[r * 3] * gxa;
+        }
+        R Tw[3] = {0, 0, 0}, Tv[3] = {0, 0, 0}, Tgy[3] = {0, 0, 0}, Tgz[3] = {0, 0, 0};
+        R Sww = 0, Ssw = 0, Sws = 0;
 #pragma unroll
         for (int b = 0; b < K; ++b) {
             const int j = sn.base[1] + b;
             if ((unsigned)j >= (unsigned)kp.dims[1]) continue;
+            const R gyb = sn.g[1][b];
+            R Pab[3], Qab[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                Pab[r] = Pa[r] + A[r * 3 + 1] * gyb;
+                Qab[r] = Qa[r] + CC[r * 3 + 1] * gyb;
+            }
+            R U[3] = {0, 0, 0}, UV[3] = {0, 0, 0}, Ug[3] = {0, 0, 0};
+            R Vw = 0, Vs = 0;
             const long long row = ((long long)i * kp.dims[1] + j) * kp.dims[2];
-            const R wab = sn.w[0][a] * sn.w[1][b];
-            const R gwx_ab = nidx * sn.s[0][a] * sn.w[1][b], gwy_ab = nidx * sn.w[0][a] * sn.s[1][b];
-            const R dgx = sn.g[0][a], dgy = sn.g[1][b];
+            const int trow = tl.on ? tl.index(i, j, 0) : 0;  // + k gives index(i, j, k)
 #pragma unroll
             for (int c = 0; c < K; ++c) {
                 const int k = sn.base[2] + c;
                 if ((unsigned)k >= (unsigned)kp.dims[2]) continue;
                 R d[4], vi[3];
-                load_node4(adj, row + k, d);
-                load_node3(grid, row + k, vi);
-                const R w = wab * sn.w[2][c];
-                const R gw0 = gwx_ab * sn.w[2][c], gw1 = gwy_ab * sn.w[2][c], gw2 = nidx * wab * sn.s[2][c];
-                const R dgz = sn.g[2][c];
-                R Adg[3], cdg[3];
+                if (tl.on) {
+                    const float4 qa = ta[trow + k], qg = tg[trow + k];
+                    d[0] = (R)qa.x;
+                    d[1] = (R)qa.y;
+                    d[2] = (R)qa.z;
+                    d[3] = (R)qa.w;
+                    vi[0] = (R)qg.x;
+                    vi[1] = (R)qg.y;
+                    vi[2] = (R)qg.z;
+                } else {
+                    load_node4(adj, row + k, d);
+                    load_node3(grid, row + k, vi);
+                }
+                const R gzc = sn.g[2][c], wc = sn.w[2][c];
+                R sig = mass * d[3];
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
-                    Adg[r] = A[r * 3] * dgx + A[r * 3 + 1] * dgy + A[r * 3 + 2] * dgz;
-                    cdg[r] = CC[r * 3] * dgx + CC[r * 3 + 1] * dgy + CC[r * 3 + 2] * dgz;
+                    sig += (Pab[r] + A[r * 3 + 2] * gzc) * d[r];
+                    sig += vi[r] * (Qab[r] + CC[r * 3 + 2] * gzc);
                 }
-                const R sig = mass * d[3] + (mvv[0] + Adg[0]) * d[0] + (mvv[1] + Adg[1]) * d[1] +
-                              (mvv[2] + Adg[2]) * d[2] + vi[0] * (o.vbar[0] + cdg[0]) +
-                              vi[1] * (o.vbar[1] + cdg[1]) + vi[2] * (o.vbar[2] + cdg[2]);
-                ax[0] += sig * gw0;
-                ax[1] += sig * gw1;
-                ax[2] += sig * gw2;
+                const R wcg = wc * gzc;
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
-                    const R wd = w * d[r];
-                    bp[r] += wd;
-                    bv[r] += w * vi[r];
-                    M1[r * 3 + 0] += wd * dgx;
-                    M1[r * 3 + 1] += wd * dgy;
-                    M1[r * 3 + 2] += wd * dgz;
+                    U[r] += wc * d[r];
+                    UV[r] += wc * vi[r];
+                    Ug[r] += wcg * d[r];
                 }
+                Vw += wc * sig;
+                Vs += sn.s[2][c] * sig;
             }
+            const R wb = sn.w[1][b], wbg = wb * gyb;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                Tw[r] += wb * U[r];
+                Tv[r] += wb * UV[r];
+                Tgy[r] += wbg * U[r];
+                Tgz[r] += wb * Ug[r];
+            }
+            Sww += wb * Vw;
+            Ssw += sn.s[1][b] * Vw;
+            Sws += wb * Vs;
         }
+        const R wa = sn.w[0][a], wag = wa * gxa;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            bp[r] += wa * Tw[r];
+            bv[r] += wa * Tv[r];
+            M1[r * 3 + 0] += wag * Tw[r];
+            M1[r * 3 + 1] += wa * Tgy[r];
+            M1[r * 3 + 2] += wa * Tgz[r];
+        }
+        ax[0] += sn.s[0][a] * Sww;
+        ax[1] += wa * Ssw;
+        ax[2] += wa * Sws;
     }
+    {
+        const R nidx = -kp.inv_dx;
+        ax[0] *= nidx;
+        ax[1] *= nidx;
+        ax[2] *= nidx;
+    }
+    if (!valid) return;
     R gx1[3];
     load_planes(g1 + ST_X * ld, ld, p, 3, gx1);
     R gx[3], gv[3];
@@ -1292,6 +1409,21 @@ int tile_cap_for()
 
 // ----------------------------------------------------------- launchers
 
+// Raise a kernel's dynamic shared-memory limit once (the attribute is
+// persistent; setting it before every launch costs host time per launch).
+template <typename KernelT>
+void ensure_smem(KernelT* kernel, size_t bytes)
+{
+    // keyed by kernel address: instantiations can share one function type
+    static std::unordered_map<const void*, size_t> done;
+    size_t& cur = done[reinterpret_cast<const void*>(kernel)];
+    if (bytes > cur) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cur = bytes;
+    }
+}
+
+
 template <typename R>
 void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
                 cudaStream_t s)
@@ -1303,10 +1435,10 @@ void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
         if (g_scatter_mode == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 4);
             if (c.kernel == 0) {
-                cudaFuncSetAttribute(k_p2g_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                ensure_smem(k_p2g_seg<4>, sm);
                 k_p2g_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
             } else {
-                cudaFuncSetAttribute(k_p2g_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                ensure_smem(k_p2g_seg<3>, sm);
                 k_p2g_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
             }
             return;
@@ -1345,10 +1477,10 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
         if (g_scatter_mode == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 3);
             if (c.kernel == 0) {
-                cudaFuncSetAttribute(k_g2p_adj_seg<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                ensure_smem(k_g2p_adj_seg<4>, sm);
                 k_g2p_adj_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             } else {
-                cudaFuncSetAttribute(k_g2p_adj_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                ensure_smem(k_g2p_adj_seg<3>, sm);
                 k_g2p_adj_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             }
             return;
@@ -1373,12 +1505,17 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
-    if (c.kernel == 0)
-        k_p2g_adj<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
-                                                         glam, gmu);
-    else
-        k_p2g_adj<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
-                                                         glam, gmu);
+    const int cap = tile_cap_for<R>();
+    const size_t sm = (size_t)cap * 2 * sizeof(float4);
+    if (c.kernel == 0) {
+        ensure_smem(k_p2g_adj<R, 4>, sm);
+        k_p2g_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+                                                          glam, gmu, cap);
+    } else {
+        ensure_smem(k_p2g_adj<R, 3>, sm);
+        k_p2g_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+                                                          glam, gmu, cap);
+    }
 }
 
 template <typename R>

@@ -144,8 +144,74 @@ struct Stencil {
     R g[3][K];
 };
 
+// FP32 stencil from the fractional cell coordinate f: each stencil offset
+// always falls on the same piece of the spline, so weights and slopes are
+// fixed polynomials in f (no divides, no branches), and dg = (o - 1 - f) dx
+// (cubic) or (o - f) dx (quadratic).  Same values as Interpolation.h:5-30
+// evaluated at dg/dx, up to FP32 rounding.
+template <int K>
+MPM_HD void make_stencil_poly(const float* x, const float* gmin, float dx, float inv_dx, Stencil<float, K>& st,
+                              bool want_slope)
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float rel = (x[a] - gmin[a]) * inv_dx;
+        if (K == 4) {
+            const float fl = floorf(rel);
+            const float f = rel - fl, g = 1.f - f;
+            const float f2 = f * f, g2 = g * g;
+            st.base[a] = (int)fl - 1;
+            st.w[a][0] = g2 * g * (1.f / 6.f);
+            st.w[a][1] = (0.5f * f - 1.f) * f2 + (2.f / 3.f);
+            st.w[a][2] = (0.5f * g - 1.f) * g2 + (2.f / 3.f);
+            st.w[a][K - 1] = f2 * f * (1.f / 6.f);
+            st.g[a][0] = (-1.f - f) * dx;
+            st.g[a][1] = -f * dx;
+            st.g[a][2] = g * dx;
+            st.g[a][K - 1] = (2.f - f) * dx;
+            if (want_slope) {
+                st.s[a][0] = 0.5f * g2;
+                st.s[a][1] = (2.f - 1.5f * f) * f;
+                st.s[a][2] = (1.5f * g - 2.f) * g;
+                st.s[a][K - 1] = -0.5f * f2;
+            }
+        } else {
+            const float fl = floorf(rel - 0.5f);
+            const float f = rel - fl;  // in [0.5, 1.5)
+            const float u = 1.5f - f, v = f - 1.f, z = f - 0.5f;
+            st.base[a] = (int)fl;
+            st.w[a][0] = 0.5f * u * u;
+            st.w[a][1] = 0.75f - v * v;
+            st.w[a][2] = 0.5f * z * z;
+            st.g[a][0] = -f * dx;
+            st.g[a][1] = (1.f - f) * dx;
+            st.g[a][2] = (2.f - f) * dx;
+            if (want_slope) {
+                st.s[a][0] = u;
+                st.s[a][1] = 2.f * v;
+                st.s[a][2] = -z;
+            }
+        }
+        if (!want_slope)
+#pragma unroll
+            for (int o = 0; o < K; ++o) st.s[a][o] = 0.f;
+    }
+}
+
+template <typename R, int K>
+MPM_HD void make_stencil_ref(const R* x, const R* gmin, R dx, R inv_dx, Stencil<R, K>& st, bool want_slope);
+
+// Stencil of particle x: the FP32 path uses the polynomial form above, the
+// FP64 path the reference's own sequence (node position, dg, N(dg/dx)).
 template <typename R, int K>
 MPM_HD void make_stencil(const R* x, const R* gmin, R dx, R inv_dx, Stencil<R, K>& st, bool want_slope)
+{
+    if constexpr (sizeof(R) == 4) make_stencil_poly<K>(x, gmin, dx, inv_dx, st, want_slope);
+    else make_stencil_ref<R, K>(x, gmin, dx, inv_dx, st, want_slope);
+}
+
+template <typename R, int K>
+MPM_HD void make_stencil_ref(const R* x, const R* gmin, R dx, R inv_dx, Stencil<R, K>& st, bool want_slope)
 {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -162,6 +228,37 @@ MPM_HD void make_stencil(const R* x, const R* gmin, R dx, R inv_dx, Stencil<R, K
             st.s[a][o] = want_slope ? sl : R(0);
         }
     }
+}
+
+// Reciprocal: correctly rounded in both precisions, but for FP32 without
+// the full IEEE division sequence.
+MPM_HD float rcp(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.f / x;
+#endif
+}
+MPM_HD double rcp(double x) { return 1.0 / x; }
+
+// x^(1/4) and x^(-1/4) for the Newton scaling factor, which only needs to be
+// approximate (it accelerates convergence; it does not change the limit).
+MPM_HD void quarter_pow(float x, float& g, float& ig)
+{
+#ifdef __CUDA_ARCH__
+    const float r = rsqrtf(x);  // x^-1/2
+    ig = sqrtf(r);              // x^-1/4
+    g = __frcp_rn(ig);
+#else
+    g = sqrtf(sqrtf(x));
+    ig = 1.f / g;
+#endif
+}
+MPM_HD void quarter_pow(double x, double& g, double& ig)
+{
+    g = sqrt(sqrt(x));
+    ig = 1.0 / g;
 }
 
 // ------------------------------------------------------------ polar / SVD
@@ -253,17 +350,20 @@ MPM_HD void polar_svd(const double* F, double* Rm)
         for (int c = 0; c < 3; ++c) Rm[r * 3 + c] = u[0][r] * Vs[c * 3] + u[1][r] * Vs[c * 3 + 1] + u[2][r] * Vs[c * 3 + 2];
 }
 
+// Newton stopping rule: once the relative step is below `step` (squared
+// here), one more step is taken; convergence is quadratic, so that last step
+// lands below the precision's rounding level.
 template <typename R>
 struct Tol;
 template <>
 struct Tol<float> {
-    static constexpr float newton = 1e-13f;  // squared relative step
-    static constexpr int iters = 12;
+    static constexpr float step2 = 1e-10f;
+    static constexpr int iters = 10;
 };
 template <>
 struct Tol<double> {
-    static constexpr double newton = 1e-30;
-    static constexpr int iters = 40;
+    static constexpr double step2 = 1e-16;
+    static constexpr int iters = 30;
 };
 
 // Scaled Newton iteration for the polar factor (Higham 1986):
@@ -275,18 +375,17 @@ MPM_HD bool polar_newton(const R* F, R* Rm)
     R X[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) X[i] = F[i];
-    bool scale = true;
+    bool scale = true, last = false;
     for (int it = 0; it < Tol<R>::iters; ++it) {
         R c[9];
         cof3(X, c);
         R d = X[0] * c[0] + X[1] * c[1] + X[2] * c[2];
         if (!(d > R(0))) return false;
-        R inv_d = R(1) / d;
+        R inv_d = rcp(d);
         R g = R(1), ig = R(1);
         if (scale) {
             R nx = dot9(X, X), nc = dot9(c, c) * inv_d * inv_d;
-            g = sqrt(sqrt(nc / nx));
-            ig = R(1) / g;
+            quarter_pow(nc * rcp(nx), g, ig);
         }
         R diff = 0, ny = 0;
 #pragma unroll
@@ -298,11 +397,8 @@ MPM_HD bool polar_newton(const R* F, R* Rm)
             X[i] = y;
         }
         if (diff < R(1e-4)) scale = false;
-        if (diff <= Tol<R>::newton * ny) {
-#pragma unroll
-            for (int i = 0; i < 9; ++i) Rm[i] = X[i];
-            return true;
-        }
+        if (last) break;
+        if (diff <= Tol<R>::step2 * ny) last = true;
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) Rm[i] = X[i];
@@ -353,7 +449,7 @@ MPM_HD void invariants(const R* F, Inv<R>& v)
     if (J > R(0.25)) {
         R c[9];
         cof3(F, c);
-        R inv = R(1) / J;
+        R inv = rcp(J);
 #pragma unroll
         for (int i = 0; i < 9; ++i) v.Fit[i] = c[i] * inv;
         v.Jraw = J;
@@ -423,7 +519,7 @@ MPM_HD void pk_vjp(int material, bool exact, const R* F, R lam, R mu, const Inv<
         R b3[3] = {rg[7] - rg[5], rg[2] - rg[6], rg[3] - rg[1]};
         R c[9];
         cof3(A, c);
-        R idet = R(1) / (A[0] * c[0] + A[1] * c[1] + A[2] * c[2]);
+        R idet = rcp(A[0] * c[0] + A[1] * c[1] + A[2] * c[2]);
         R w0 = (c[0] * b3[0] + c[3] * b3[1] + c[6] * b3[2]) * idet;
         R w1 = (c[1] * b3[0] + c[4] * b3[1] + c[7] * b3[2]) * idet;
         R w2 = (c[2] * b3[0] + c[5] * b3[1] + c[8] * b3[2]) * idet;
