@@ -1014,6 +1014,8 @@ void check_cg(const mpm_compgraph* cg)
 
 }  // namespace
 
+void mpm::set_last_error(const char* msg) { g_err = msg; }
+
 // ===================================================================== C ABI
 
 extern "C" {

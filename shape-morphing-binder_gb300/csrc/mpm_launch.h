@@ -90,4 +90,7 @@ void launch_count_active(const StepCfg& c, const R* grid, unsigned long long* ou
 template <typename R>
 void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStream_t s);
 
+// record the message mpm_last_error() returns on this host thread
+void set_last_error(const char* msg);
+
 }  // namespace mpm

@@ -100,6 +100,7 @@ _SIGS = {
     "mpm_profile_query": [C.c_int, C.POINTER(C.c_longlong), _dp],
     "mpm_kernel_name": [C.c_int],
     "mpm_launch_count": [],
+    "mpm_mass_loss_noalloc": [C.c_int, _vp, _vp, _vp, _ip, C.c_double, _dp, C.c_int, _vp, _dp, _vp],
 }
 _RESTYPE = {"mpm_last_error": C.c_char_p, "mpm_kernel_name": C.c_char_p, "mpm_launch_count": C.c_longlong, "mpm_default_params": None, "mpm_default_options": None,
             "mpm_set_verbose": None}
