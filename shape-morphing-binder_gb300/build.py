@@ -29,6 +29,8 @@ def flags(debug: bool = False):
          "--expt-relaxed-constexpr", "-Xptxas", "-v" if os.environ.get("MPM_PTXAS_V") else "-O3"]
     if debug:
         f += ["-DMPM_DEBUG"]
+    # extra compile flags (tuning experiments), e.g. MPM_NVCC_FLAGS="-DMPM_P2G_MIN_BLOCKS=2"
+    f += os.environ.get("MPM_NVCC_FLAGS", "").split()
     return f
 
 
@@ -38,7 +40,7 @@ def _inputs():
 
 
 def up_to_date() -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or os.environ.get("MPM_NVCC_FLAGS"):
         return False
     t = LIB.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _inputs())

@@ -23,6 +23,15 @@
 
 namespace mpm {
 
+// resident blocks per SM the register allocator targets for the two
+// heaviest kernels (compile-time tuning knobs)
+#ifndef MPM_P2G_MIN_BLOCKS
+#define MPM_P2G_MIN_BLOCKS 3
+#endif
+#ifndef MPM_P2G_ADJ_MIN_BLOCKS
+#define MPM_P2G_ADJ_MIN_BLOCKS 1
+#endif
+
 int g_tile_nodes = 2048;
 int g_scatter_mode = 1;
 
@@ -794,7 +803,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj(KP<R> kp, int n, long long
 
 // P_op_1 + P2G with the segmented scatter (FP32 path)
 template <int K>
-__global__ void __launch_bounds__(kThreads) k_p2g_seg(KP<float> kp, int n, long long ld, const float* __restrict__ st,
+__global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<float> kp, int n, long long ld, const float* __restrict__ st,
                                                        const float* __restrict__ dfc, const float* __restrict__ co,
                                                        float* __restrict__ grid, int tile_cap)
 {
@@ -884,7 +893,7 @@ __global__ void k_grid_adj(KP<R> kp, long long nn, const R* __restrict__ grid, R
 
 // P2G^T + P_op_1^T (BackPropagation.cpp:76-143)
 template <typename R, int K>
-__global__ void __launch_bounds__(kThreads) k_p2g_adj(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+__global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP<R> kp, int n, long long ld, const R* __restrict__ st,
                                                        const R* __restrict__ dfc, const R* __restrict__ co,
                                                        const R* __restrict__ st1, const R* __restrict__ g1,
                                                        const R* __restrict__ trust, const R* __restrict__ grid,
