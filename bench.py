@@ -154,9 +154,45 @@ def device_rollout(torch, cg, T, tgt, n):
     cg.compute_forward_pass(0, 0)
     last = cg.get_point_cloud(T)
     xT = last.get_torch("x", device="cuda")
+    # (in a batch the padding between instances has x = target = 0: zero gradient)
     g = (2.0 / n) * (xT - tgt)
     last.set("grad_x", g)
     cg.compute_backward_pass(0)
+
+
+class BatchWorkload:
+    """BASELINE configuration 3 as one workload: 64 instances concatenated."""
+
+    def __init__(self, quick=False, timesteps=0):
+        from diffmpm_bindings import workloads as W
+        self.parts = W.batched(count=8 if quick else 64, steps=10 if quick else 50)
+        self.name = "batched64" if not quick else "batched8"
+        self.steps = timesteps or self.parts[0].steps
+        self.checkpoint = 10
+        self.dt, self.drag, self.smoothing = self.parts[0].dt, 0.0, 0.0
+        self.n = sum(p.n for p in self.parts)
+        self.dims = (0, 0, 0)
+        self.dx = None
+        self.rho = float("nan")
+        self.extra = {"E": "log-U[1e3,1e5]", "nu": "U[0.2,0.45]"}
+
+
+def build_batch_graph(dm, bw, precision):
+    dt = np.float64 if precision == "fp64" else np.float32
+    pcs, grids = [], []
+    for w in bw.parts:
+        pcs.append(dm.PointCloud.from_arrays(w.x.astype(dt), v=w.v.astype(dt), F=w.F.astype(dt), m=w.m.astype(dt),
+                                             vol=w.vol.astype(dt), lam=w.lam.astype(dt), mu=w.mu.astype(dt),
+                                             precision=precision))
+        grids.append(dm.Grid(*w.dims, w.dx, w.grid_min, precision=precision))
+    cg = dm.CompGraph.batch(pcs, grids, adjoint="exact", checkpoint_every=bw.checkpoint)
+    cg.set_sim_params(dt=bw.dt, drag=bw.drag, smoothing=bw.smoothing)
+    n_pad = len(cg.get_point_cloud(0))
+    tgt = np.zeros((n_pad, 3))
+    rng = np.random.default_rng(11)
+    for i, w in enumerate(bw.parts):
+        tgt[cg.instance_range(i)] = w.x + 0.01 * rng.normal(size=w.x.shape)
+    return cg, (pcs, grids), tgt, n_pad
 
 
 def run_ours(args, rank, world, device):
@@ -164,9 +200,17 @@ def run_ours(args, rank, world, device):
     import diffmpm_bindings as dm
     lib = dm._lib.lib
     lib.mpm_set_verbose(0)
-    w = make_workload(args.workload, args.quick, args.timesteps)
-    n, T = w.n, w.steps
-    cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
+    if args.workload == "batched":
+        w = BatchWorkload(args.quick, args.timesteps)
+        n, T = w.n, w.steps
+        cg, keep, tgt_np, n_pad = build_batch_graph(dm, w, "fp32")
+        w.target = tgt_np
+        args.no_e2e, args.no_fp64, args.no_cpu = True, True, True
+    else:
+        w = make_workload(args.workload, args.quick, args.timesteps)
+        n, T = w.n, w.steps
+        cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
+        n_pad = n
     cg.set_up_comp_graph(T + 1)
     stream = torch.cuda.current_stream(device)
     cg.set_stream(stream)
@@ -245,6 +289,7 @@ def run_ours(args, rank, world, device):
         "warmup": args.warmup, "ms_per_step": round(1e3 * t_total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64-guarded stress)", "data": "synthetic (seeded)",
         "config": {"workload": w.name, "particles": n, "grid_nodes": list(w.dims), "dx": w.dx, "timesteps": T,
+                   "instances": len(w.parts) if hasattr(w, "parts") else 1,
                    "checkpoint_every": w.checkpoint, "dt": w.dt, "density": round(w.rho, 3),
                    "material": "fixed-corotated E=%g nu=%g" % (w.extra["E"], w.extra["nu"]),
                    "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
@@ -419,7 +464,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spheres2m", choices=["spheres2m", "ellipsoid64", "sphere32"])
+    ap.add_argument("--workload", default="spheres2m", choices=["spheres2m", "ellipsoid64", "sphere32", "batched"])
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-particles", type=int, default=0, help="0: every particle")
     ap.add_argument("--cpu-timesteps", type=int, default=2)

@@ -151,6 +151,21 @@ int mpm_calculate_point_cloud_volumes(mpm_pointcloud* pc, mpm_grid* g);
 int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_grid* target_grid,
                          const mpm_options* opt, mpm_compgraph** out);
 int mpm_compgraph_release(mpm_compgraph* cg);
+/* No counterpart in the reference (BASELINE configuration 3): a CompGraph
+ * over `count` independent instances, each with its own particles and grid
+ * (uneven sizes allowed), advanced together -- every kernel launch covers
+ * all instances through per-instance particle and node offsets.  dt, drag,
+ * smoothing, f_ext and the options are shared.  Layer views hold the
+ * instances' particles concatenated; mpm_compgraph_batch_offsets gives where
+ * instance i starts (particle_offsets[i], multiples of 256; its particles
+ * are [particle_offsets[i], particle_offsets[i] + n_i)).  The mass loss is
+ * not defined for batches. */
+int mpm_compgraph_create_batch(const mpm_pointcloud* const* pcs, const mpm_grid* const* grids, int count,
+                               const mpm_options* opt, mpm_compgraph** out);
+/* count of instances (0: not a batch) and offsets (arrays of count+1; the
+ * last particle entry is the end of the last instance's particles) */
+int mpm_compgraph_batch_offsets(const mpm_compgraph* cg, int* count, long long* particle_offsets,
+                                long long* node_offsets);
 /* dt, drag, smoothing, f_ext (private in CompGraph.h:78-83; additive setter) */
 int mpm_compgraph_set_params(mpm_compgraph* cg, const mpm_params* p);
 int mpm_compgraph_get_params(const mpm_compgraph* cg, mpm_params* p);

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -518,6 +519,10 @@ struct Graph {
     std::vector<Buf> sgrid, strust;                 // recomputed segment grids
     bool lame_on = false;                           // accumulate dL/dlam, dL/dmu
     Buf glame;                                      // 2 planes
+    // batch of independent instances (empty: one instance)
+    std::vector<InstHost> inst;
+    Buf inst_table;
+    long long total_nodes = 0;
     // render gradients (stored on the host like CompGraph.h:73-76)
     std::vector<float> rgF, rgx;
     bool has_rg = false;
@@ -543,6 +548,11 @@ struct Graph {
         c.kernel = opt.kernel;
         c.material = opt.material;
         c.exact = opt.adjoint == MPM_ADJ_EXACT;
+        if (!inst.empty()) {
+            c.inst = inst_table->p;
+            c.ninst = (int)inst.size();
+            c.total_nodes = total_nodes;
+        }
         return c;
     }
 
@@ -777,6 +787,7 @@ void graph_backward(Graph& G, int control)
 template <typename R>
 double graph_loss(Graph& G)
 {
+    if (!G.inst.empty()) fail(MPM_ERR_STATE, "the mass loss is defined for single-instance graphs");
     if (!G.target) fail(MPM_ERR_STATE, "CompGraph has no target grid");
     if (G.target->prec != G.prec) fail(MPM_ERR_ARG, "target grid precision differs from the graph's");
     for (int a = 0; a < 3; ++a)
@@ -1268,6 +1279,111 @@ int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_gri
         G.layers[0].pc = G.base;
         ck(cudaStreamSynchronize(G.stream), "sync");
         *out = cg.release();
+    });
+}
+
+int mpm_compgraph_create_batch(const mpm_pointcloud* const* pcs, const mpm_grid* const* grids, int count,
+                               const mpm_options* opt, mpm_compgraph** out)
+{
+    return guard([&] {
+        if (!pcs || !grids || count <= 0 || !out) fail(MPM_ERR_ARG, "bad batch arguments");
+        for (int i = 0; i < count; ++i) {
+            check_pc(pcs[i]);
+            check_grid(grids[i]);
+        }
+        std::unique_ptr<mpm_compgraph> cg(new mpm_compgraph());
+        Graph& G = cg->g;
+        mpm_default_options(&G.opt);
+        if (opt) G.opt = *opt;
+        if (G.opt.checkpoint_every < 1) G.opt.checkpoint_every = 1;
+        mpm_default_params(&G.prm);
+        G.prec = pcs[0]->d->prec;
+        if (G.opt.precision != G.prec) fail(MPM_ERR_ARG, "options.precision differs from the PointClouds'");
+        const long long B = 256;  // particle ranges start at multiples of the kernels' block size
+        long long poff = 0, goff = 0;
+        G.inst.resize(count);
+        for (int i = 0; i < count; ++i) {
+            const PCData& d = *pcs[i]->d;
+            const GridData& g = *grids[i]->d;
+            if (d.prec != G.prec || g.prec != G.prec) fail(MPM_ERR_ARG, "instance %d precision differs", i);
+            if (d.n <= 0) fail(MPM_ERR_SHAPE, "instance %d has no particles", i);
+            InstHost& h = G.inst[i];
+            for (int a = 0; a < 3; ++a) {
+                h.dims[a] = g.dims[a];
+                h.gmin[a] = g.gmin[a];
+            }
+            h.dx = g.dx;
+            h.n = d.n;
+            h.poff = poff;
+            h.goff = goff;
+            poff += (d.n + B - 1) / B * B;
+            goff += g.nn();
+        }
+        if (poff > INT_MAX) fail(MPM_ERR_SHAPE, "batch holds too many particles");
+        G.total_nodes = goff;
+        ck(cudaStreamCreateWithFlags(&G.own, cudaStreamNonBlocking), "cudaStreamCreate");
+        G.stream = G.own;
+        cudaStream_t s = G.stream;
+        const GridData& g0 = *grids[0]->d;
+        G.geom.prec = G.prec;
+        for (int a = 0; a < 3; ++a) {
+            G.geom.dims[a] = g0.dims[a];
+            G.geom.gmin[a] = g0.gmin[a];
+        }
+        G.geom.dx = g0.dx;
+        G.inst_table = make_buf(inst_table_bytes(count, (int)esize(G.prec)), s, false);
+        make_inst_table(G.inst.data(), count, G.opt.kernel, (int)esize(G.prec), G.inst_table->p, s);
+        // concatenate the instances plane by plane
+        auto base = std::make_shared<PCData>();
+        base->n = (int)poff;
+        base->ld = pad_ld(base->n);
+        base->prec = G.prec;
+        base->st = make_buf(base->planes_bytes(ST_N), s, true);
+        base->co = make_buf(base->planes_bytes(CO_N), s, true);
+        base->dfc = make_buf(base->planes_bytes(9), s, true);
+        bool any_dfc = false;
+        const size_t es = esize(G.prec);
+        for (int i = 0; i < count; ++i) {
+            const PCData& d = *pcs[i]->d;
+            ck(cudaStreamSynchronize(pcs[i]->stream), "sync");
+            const size_t off = (size_t)G.inst[i].poff * es, bytes = (size_t)d.n * es;
+            auto copy_planes = [&](const Buf& dst, const Buf& src, int k, long long ldst) {
+                ck(cudaMemcpy2DAsync(dst->as<char>() + off, (size_t)ldst * es, src->as<char>(), (size_t)d.ld * es, bytes,
+                                     k, cudaMemcpyDeviceToDevice, s),
+                   "cudaMemcpy2DAsync");
+            };
+            copy_planes(base->st, d.st, ST_N, base->ld);
+            copy_planes(base->co, d.co, CO_N, base->ld);
+            if (!d.dfc_zero) {
+                copy_planes(base->dfc, d.dfc, 9, base->ld);
+                any_dfc = true;
+            }
+        }
+        base->dfc_zero = !any_dfc;
+        ck(cudaStreamSynchronize(s), "sync");
+        G.base = base;
+        G.layers.resize(1);
+        G.layers[0].pc = G.base;
+        *out = cg.release();
+    });
+}
+
+int mpm_compgraph_batch_offsets(const mpm_compgraph* cg, int* count, long long* particle_offsets,
+                                long long* node_offsets)
+{
+    return guard([&] {
+        check_cg(cg);
+        const Graph& G = cg->g;
+        const int c = (int)G.inst.size();
+        if (count) *count = c;
+        for (int i = 0; i < c; ++i) {
+            if (particle_offsets) particle_offsets[i] = G.inst[i].poff;
+            if (node_offsets) node_offsets[i] = G.inst[i].goff;
+        }
+        if (c > 0) {
+            if (particle_offsets) particle_offsets[c] = G.inst[c - 1].poff + G.inst[c - 1].n;
+            if (node_offsets) node_offsets[c] = G.total_nodes;
+        }
     });
 }
 

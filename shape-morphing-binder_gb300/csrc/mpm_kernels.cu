@@ -17,6 +17,7 @@
 #include <climits>
 #include <cstdint>
 #include <unordered_map>
+#include <vector>
 
 #include "mpm_launch.h"
 #include "mpm_math.cuh"
@@ -39,12 +40,25 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// One instance of a batch: its grid and its particle range.  Particle
+// ranges start at multiples of the block size, so a block never straddles
+// two instances.
+template <typename R>
+struct InstDev {
+    R dx, inv_dx, C0, gmin[3];
+    int dims[3];
+    int n;
+    long long poff, goff;
+};
+
 template <typename R>
 struct KP {
     R dt, dragf, s, bulk, jmin, C0, dx, inv_dx;
     R gmin[3], dtf[3];
     int dims[3];
     int material, exact;
+    const InstDev<R>* inst;  // null: one instance described by the fields above
+    int ninst;
 };
 
 template <typename R>
@@ -66,7 +80,36 @@ KP<R> make_kp(const StepCfg& c)
     }
     k.material = c.material;
     k.exact = c.exact;
+    k.inst = static_cast<const InstDev<R>*>(c.inst);
+    k.ninst = c.ninst;
     return k;
+}
+
+// Batched launches: point kp at the block's instance and return the end of
+// its particle range and its first grid node.
+template <typename R>
+MPM_D void bind_instance(KP<R>& kp, int& n_end, long long& goff)
+{
+    goff = 0;
+    if (!kp.inst) return;
+    const long long p0 = (long long)blockIdx.x * blockDim.x;
+    int lo = 0, hi = kp.ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (kp.inst[mid].poff <= p0) lo = mid;
+        else hi = mid - 1;
+    }
+    const InstDev<R>& I = kp.inst[lo];
+    kp.dx = I.dx;
+    kp.inv_dx = I.inv_dx;
+    kp.C0 = I.C0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        kp.gmin[a] = I.gmin[a];
+        kp.dims[a] = I.dims[a];
+    }
+    n_end = (int)(I.poff + I.n);
+    goff = I.goff;
 }
 
 inline int nblocks(long long n, int t = kThreads) { return (int)((n + t - 1) / t); }
@@ -428,6 +471,9 @@ __global__ void __launch_bounds__(kThreads) k_p2g(KP<R> kp, int n, long long ld,
                                                    R* __restrict__ grid, int tile_cap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
     Stencil<R, K> sten;
@@ -646,6 +692,9 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KP<R> kp, int n, long long ld,
                                                    const R* __restrict__ dfc, const R* __restrict__ grid,
                                                    R* __restrict__ st1, R* __restrict__ trust)
 {
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     R x[3], F[9], Ft[9];
@@ -772,6 +821,9 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj(KP<R> kp, int n, long long
                                                        R* __restrict__ adj, int tile_cap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    adj += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
     Stencil<R, K> sten;
@@ -808,6 +860,9 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<flo
                                                        float* __restrict__ grid, int tile_cap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
     Stencil<float, K> sten;
@@ -845,6 +900,9 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj_seg(KP<float> kp, int n, l
                                                            int tile_cap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    adj += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
     Stencil<float, K> sten;
@@ -902,7 +960,11 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP
                                                        R* __restrict__ gmu, int cap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    // tail threads of the last block mirror particle n-1 (never stored) so the
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
+    adj += goff * 4;
+    // tail threads of the block mirror particle n-1 (never stored) so the
     // whole block can take part in staging the node tile
     const int p_raw = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p_raw < n;
@@ -1417,6 +1479,45 @@ int tile_cap_for()
 }  // namespace
 
 // ----------------------------------------------------------- launchers
+
+template <typename R>
+static void fill_table(const InstHost* h, int count, int kernel, std::vector<InstDev<R>>& out)
+{
+    out.resize(count);
+    for (int i = 0; i < count; ++i) {
+        InstDev<R>& d = out[i];
+        d.dx = (R)h[i].dx;
+        d.inv_dx = (R)(1.0 / h[i].dx);
+        d.C0 = (R)((kernel == 0 ? 3.0 : 4.0) / (h[i].dx * h[i].dx));
+        for (int a = 0; a < 3; ++a) {
+            d.gmin[a] = (R)h[i].gmin[a];
+            d.dims[a] = h[i].dims[a];
+        }
+        d.n = h[i].n;
+        d.poff = h[i].poff;
+        d.goff = h[i].goff;
+    }
+}
+
+size_t inst_table_bytes(int count, int prec_bytes)
+{
+    return (size_t)count * (prec_bytes == 8 ? sizeof(InstDev<double>) : sizeof(InstDev<float>));
+}
+
+void make_inst_table(const InstHost* h, int count, int kernel, int prec_bytes, void* dst, cudaStream_t s)
+{
+    if (prec_bytes == 8) {
+        std::vector<InstDev<double>> t;
+        fill_table(h, count, kernel, t);
+        cudaMemcpyAsync(dst, t.data(), t.size() * sizeof(t[0]), cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+    } else {
+        std::vector<InstDev<float>> t;
+        fill_table(h, count, kernel, t);
+        cudaMemcpyAsync(dst, t.data(), t.size() * sizeof(t[0]), cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+    }
+}
 
 // Raise a kernel's dynamic shared-memory limit once (the attribute is
 // persistent; setting it before every launch costs host time per launch).

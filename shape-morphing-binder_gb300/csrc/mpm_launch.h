@@ -27,8 +27,24 @@ struct StepCfg {
     int kernel = 0;    // 0 cubic B-spline, 1 quadratic
     int material = 0;  // 0 fixed-corotated, 1 Neo-Hookean
     int exact = 0;     // 0 reference-compatible adjoint, 1 exact adjoint
-    long long nodes() const { return (long long)dims[0] * dims[1] * dims[2]; }
+    // batched launches: device table of InstDev<R> (one per instance) and the
+    // total node count of the concatenated grids; null for one instance
+    const void* inst = nullptr;
+    int ninst = 0;
+    long long total_nodes = 0;
+    long long nodes() const { return inst ? total_nodes : (long long)dims[0] * dims[1] * dims[2]; }
 };
+
+// host mirror of one batch instance (converted to the kernels' table)
+struct InstHost {
+    int dims[3];
+    double dx, gmin[3];
+    int n;
+    long long poff, goff;
+};
+// builds the device table for precision R (sizeof(R) 4 or 8) into dst
+void make_inst_table(const InstHost* h, int count, int kernel, int prec_bytes, void* dst, cudaStream_t s);
+size_t inst_table_bytes(int count, int prec_bytes);
 
 // Shared-memory tile budget (nodes) for the scatter kernels; 0 disables tiles.
 extern int g_tile_nodes;

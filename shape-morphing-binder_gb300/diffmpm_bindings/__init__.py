@@ -325,6 +325,41 @@ class CompGraph:
             lib.mpm_compgraph_release(h)
             self._h = None
 
+    @classmethod
+    def batch(cls, point_clouds, grids, *, adjoint="reference", kernel="cubic", material="fcr",
+              checkpoint_every=1) -> "CompGraph":
+        """Independent instances advanced together in one launch per kernel
+        (additive; BASELINE configuration 3).  ``instance_range(i)`` gives the
+        slice of instance i in the concatenated layer arrays."""
+        if len(point_clouds) != len(grids) or not point_clouds:
+            raise RuntimeError("batch needs one grid per point cloud")
+        o = MpmOptions()
+        lib.mpm_default_options(C.byref(o))
+        o.precision = point_clouds[0].precision
+        o.adjoint = {"reference": MPM_ADJ_REFERENCE, "exact": MPM_ADJ_EXACT}[adjoint]
+        o.kernel = {"cubic": MPM_KERNEL_CUBIC, "quadratic": MPM_KERNEL_QUADRATIC}[kernel]
+        o.material = {"fcr": MPM_MAT_FCR, "neohookean": MPM_MAT_NEOHOOKEAN}[material]
+        o.checkpoint_every = int(checkpoint_every)
+        k = len(point_clouds)
+        pcs = (C.c_void_p * k)(*[p._h for p in point_clouds])
+        gs = (C.c_void_p * k)(*[g._h for g in grids])
+        h = C.c_void_p()
+        check(lib.mpm_compgraph_create_batch(pcs, gs, k, C.byref(o), C.byref(h)), "CompGraph.batch")
+        self = cls.__new__(cls)
+        self._h = h
+        self._target = None
+        self._grid = list(grids)
+        self.precision = o.precision
+        cnt = C.c_int()
+        po = (C.c_longlong * (k + 1))()
+        check(lib.mpm_compgraph_batch_offsets(h, C.byref(cnt), po, None))
+        self.sizes = [len(p) for p in point_clouds]
+        self.offsets = [int(po[i]) for i in range(k)]
+        return self
+
+    def instance_range(self, i: int) -> slice:
+        return slice(self.offsets[i], self.offsets[i] + self.sizes[i])
+
     # -- additive configuration
     @property
     def options(self) -> dict:

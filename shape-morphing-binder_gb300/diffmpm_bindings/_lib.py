@@ -73,6 +73,8 @@ _SIGS = {
     "mpm_calculate_point_cloud_volumes": [_vp, _vp],
     "mpm_compgraph_create": [_vp, _vp, _vp, C.POINTER(MpmOptions), C.POINTER(_vp)],
     "mpm_compgraph_release": [_vp],
+    "mpm_compgraph_create_batch": [C.POINTER(_vp), C.POINTER(_vp), C.c_int, C.POINTER(MpmOptions), C.POINTER(_vp)],
+    "mpm_compgraph_batch_offsets": [_vp, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "mpm_compgraph_set_params": [_vp, C.POINTER(MpmParams)],
     "mpm_compgraph_get_params": [_vp, C.POINTER(MpmParams)],
     "mpm_compgraph_get_options": [_vp, C.POINTER(MpmOptions)],
