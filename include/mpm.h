@@ -222,6 +222,10 @@ const char* mpm_kernel_name(int kernel);
 /* number of engine kernels launched since the library was loaded */
 long long mpm_launch_count(void);
 
+/* record forward/backward passes as CUDA graphs and replay them (1 = on,
+ * the default): a pass is recorded the second time it runs with the same
+ * buffers and parameters and replayed from then on */
+int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on);
 /* accumulate dL/dlambda and dL/dmu per particle over the next backward
  * passes; read them from the control layer's MPM_FIELD_GRAD_LAM/GRAD_MU */
 int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on);

@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -97,7 +98,9 @@ struct Prof {
     struct Rec {
         int id;
         cudaEvent_t a, b;
+        bool graph_owned;  // recorded by a captured graph: never returned to the pool
     };
+    bool capturing = false;
     std::vector<Rec> pending;
     std::vector<cudaEvent_t> pool;
     long long count[K_COUNT] = {0};
@@ -121,8 +124,10 @@ struct Prof {
             cudaEventElapsedTime(&t, r.a, r.b);
             ms[r.id] += t;
             count[r.id] += 1;
-            pool.push_back(r.a);
-            pool.push_back(r.b);
+            if (!r.graph_owned) {
+                pool.push_back(r.a);
+                pool.push_back(r.b);
+            }
         }
         pending.clear();
     }
@@ -137,16 +142,23 @@ struct KTimer {
         g_prof.launches += k_kernels[id];
         if (g_prof.on) {
             a = g_prof.get();
-            cudaEventRecord(a, s);
+            record(a);
         }
+    }
+    // inside stream capture the event must become a graph node that records
+    // on every replay (cudaEventRecordExternal)
+    void record(cudaEvent_t e)
+    {
+        if (g_prof.capturing) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+        else cudaEventRecord(e, s);
     }
     ~KTimer()
     {
         if (a) {
             cudaEvent_t b = g_prof.get();
-            cudaEventRecord(b, s);
-            g_prof.pending.push_back({id, a, b});
-            if (g_prof.pending.size() > 4096) g_prof.resolve();
+            record(b);
+            g_prof.pending.push_back({id, a, b, g_prof.capturing});
+            if (!g_prof.capturing && g_prof.pending.size() > 4096) g_prof.resolve();
         }
     }
 };
@@ -519,6 +531,25 @@ struct Graph {
     std::vector<Buf> sgrid, strust;                 // recomputed segment grids
     bool lame_on = false;                           // accumulate dL/dlam, dL/dmu
     Buf glame;                                      // 2 planes
+    // captured forward/backward passes, keyed by pass and start layer
+    struct Cap {
+        std::vector<unsigned long long> sig;
+        int seen = 0;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0;
+        std::vector<Prof::Rec> events;
+        bool prof = false;
+        ~Cap()
+        {
+            if (exec) cudaGraphExecDestroy(exec);
+            for (auto& r : events) {
+                cudaEventDestroy(r.a);
+                cudaEventDestroy(r.b);
+            }
+        }
+    };
+    std::map<std::string, std::unique_ptr<Cap>> caps;
+    bool graphs_on = true;
     // batch of independent instances (empty: one instance)
     std::vector<InstHost> inst;
     Buf inst_table;
@@ -675,6 +706,113 @@ std::shared_ptr<PCData> shell_like(const PCData& a, cudaStream_t s, bool with_st
     return d;
 }
 
+// ------------------------------------------------------------ CUDA graphs
+// A forward or backward pass is recorded as a CUDA graph the second time it
+// runs with the same buffers and parameters (the first run allocates what it
+// needs), and replayed from then on: one cudaGraphLaunch per pass instead of
+// four launches and a memset per step.  Any change of buffers, parameters,
+// control layout or profiling state changes the signature and re-records.
+
+struct Sig {
+    std::vector<unsigned long long> v;
+    void add(unsigned long long x) { v.push_back(x); }
+    void add(const void* p) { v.push_back((unsigned long long)(uintptr_t)p); }
+    void add(const Buf& b)
+    {
+        add(b ? b->p : nullptr);
+        add(b ? (unsigned long long)b->bytes : 0ull);
+    }
+    void add_cfg(const StepCfg& c)
+    {
+        const unsigned char* p = reinterpret_cast<const unsigned char*>(&c);
+        for (size_t i = 0; i + 8 <= sizeof(StepCfg); i += 8) {
+            unsigned long long w;
+            memcpy(&w, p + i, 8);
+            v.push_back(w);
+        }
+    }
+    void add_pc(const PCData* d)
+    {
+        if (!d) {
+            add(nullptr);
+            return;
+        }
+        add(d->st);
+        add(d->grads);
+        add(d->gctl);
+        add(d->dfc_zero ? nullptr : d->dfc->p);
+        add((unsigned long long)d->have_state);
+    }
+};
+
+template <typename F>
+void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
+{
+    if (!G.graphs_on) {
+        body();
+        return;
+    }
+    sig.add((unsigned long long)g_prof.on);
+    auto& slot = G.caps[key];
+    if (!slot) slot.reset(new Graph::Cap());
+    Graph::Cap& c = *slot;
+    auto replay = [&]() {
+        ck(cudaGraphLaunch(c.exec, G.stream), "cudaGraphLaunch");
+        if (c.prof) {
+            // the graph re-records the same events: read them before the next replay
+            g_prof.pending.insert(g_prof.pending.end(), c.events.begin(), c.events.end());
+            g_prof.resolve();
+        }
+    };
+    if (c.exec && c.sig == sig.v) {
+        g_prof.launches += c.launches;
+        replay();
+        return;
+    }
+    if (c.sig != sig.v) {
+        c.sig = sig.v;
+        c.seen = 0;
+        if (c.exec) {
+            cudaGraphExecDestroy(c.exec);
+            c.exec = nullptr;
+        }
+        for (auto& r : c.events) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        c.events.clear();
+    }
+    if (c.seen++ == 0) {
+        body();  // eager: allocations and attribute setup happen here
+        return;
+    }
+    const long long l0 = g_prof.launches;
+    const size_t e0 = g_prof.pending.size();
+    ck(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    g_prof.capturing = true;
+    try {
+        body();
+    } catch (...) {
+        g_prof.capturing = false;
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(G.stream, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        g_prof.pending.resize(e0);
+        throw;
+    }
+    g_prof.capturing = false;
+    cudaGraph_t graph = nullptr;
+    ck(cudaStreamEndCapture(G.stream, &graph), "cudaStreamEndCapture");
+    cudaError_t e = cudaGraphInstantiate(&c.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    ck(e, "cudaGraphInstantiate");
+    c.launches = g_prof.launches - l0;
+    c.events.assign(g_prof.pending.begin() + e0, g_prof.pending.end());
+    g_prof.pending.resize(e0);
+    c.prof = g_prof.on;
+    replay();
+}
+
 // ComputeForwardPass (CompGraph.cpp:131-141).  With checkpointing the
 // non-stored layers pass through two scratch states and one scratch grid.
 template <typename R>
@@ -688,21 +826,41 @@ void graph_forward(Graph& G, int start)
     if (!G.layers[start].pc || !G.layers[start].pc->have_state)
         fail(MPM_ERR_STATE, "layer %d is not stored; forward passes of a checkpointed graph start at a stored layer",
              start);
-    PCData* cur = G.layers[start].pc.get();
-    for (int i = start; i < L - 1; ++i) {
-        PCData* nxt;
-        if (G.stored(i + 1)) {
-            nxt = G.layers[i + 1].pc.get();
-            if (!nxt->st) nxt->st = make_buf(cur->planes_bytes(ST_N), s, false);
-        } else {
-            auto& tmp = (cur == G.ping.get()) ? G.pong : G.ping;
-            if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
-            nxt = tmp.get();
-        }
-        if (full) step_forward<R>(c, *cur, *nxt, G.layers[i].grid, G.layers[i].trust, s);
-        else step_forward<R>(c, *cur, *nxt, G.fgrid, G.ftrust, s);
-        cur = nxt;
+    Sig sig;
+    sig.add_cfg(c);
+    sig.add((unsigned long long)L);
+    for (int i = start; i < L; ++i) {
+        sig.add_pc(G.layers[i].pc.get());
+        sig.add(G.layers[i].grid);
+        sig.add(G.layers[i].trust);
     }
+    sig.add_pc(G.ping.get());
+    sig.add_pc(G.pong.get());
+    sig.add(G.fgrid);
+    sig.add(G.ftrust);
+    run_captured(G, "fwd" + std::to_string(start), sig, [&]() {
+        PCData* cur = G.layers[start].pc.get();
+        for (int i = start; i < L - 1; ++i) {
+            PCData* nxt;
+            if (G.stored(i + 1)) {
+                nxt = G.layers[i + 1].pc.get();
+                if (!nxt->st) nxt->st = make_buf(cur->planes_bytes(ST_N), s, false);
+            } else {
+                auto& tmp = (cur == G.ping.get()) ? G.pong : G.ping;
+                if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
+                nxt = tmp.get();
+            }
+            if (full) step_forward<R>(c, *cur, *nxt, G.layers[i].grid, G.layers[i].trust, s);
+            else step_forward<R>(c, *cur, *nxt, G.fgrid, G.ftrust, s);
+            cur = nxt;
+        }
+    });
+    // layer flags set by the steps (replays do not run the host code)
+    for (int i = start + 1; i < L; ++i)
+        if (G.layers[i].pc && G.stored(i)) {
+            G.layers[i].pc->dfc_zero = true;
+            G.layers[i].pc->have_state = true;
+        }
 }
 
 template <typename R>
@@ -729,6 +887,9 @@ void inject_render_grads(Graph& G)
     say("[C++] Render gradients injected (L_tot = L_phys + L_render)\n");
 }
 
+template <typename R>
+void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s);
+
 // ComputeBackwardPass (CompGraph.cpp:143-211).  With checkpointing each
 // segment [lo, hi] between stored layers is recomputed from lo (states, grids
 // and trust scales into segment scratch) and then run backwards.
@@ -743,17 +904,42 @@ void graph_backward(Graph& G, int control)
     const int k = std::max(1, G.opt.checkpoint_every);
     if (G.lame_on) {
         PCData& ctl = *G.layers[control].pc;
-        G.glame = make_buf(ctl.planes_bytes(2), s, true);
+        ensure(G.glame, ctl.planes_bytes(2), s, false);
         ctl.glame = G.glame;
     }
-    if (k == 1) {
-        for (int i = L - 2; i >= control; --i) {
-            Layer& la = G.layers[i];
-            step_backward<R>(G, c, *la.pc, *G.layers[i + 1].pc, la.grid, la.trust, s);
-        }
-        return;
+    if (k > 1 && !G.stored(control))
+        fail(MPM_ERR_STATE, "control layer %d is not a stored layer of the checkpointed graph", control);
+    Sig sig;
+    sig.add_cfg(c);
+    sig.add((unsigned long long)L);
+    for (int i = control; i < L; ++i) {
+        sig.add_pc(G.layers[i].pc.get());
+        sig.add(G.layers[i].grid);
+        sig.add(G.layers[i].trust);
     }
-    if (!G.stored(control)) fail(MPM_ERR_STATE, "control layer %d is not a stored layer of the checkpointed graph", control);
+    sig.add(G.adj);
+    sig.add((unsigned long long)G.lame_on);
+    sig.add(G.glame);
+    sig.add_pc(G.ping.get());
+    for (auto& q : G.seg) sig.add_pc(q.get());
+    for (auto& b : G.sgrid) sig.add(b);
+    for (auto& b : G.strust) sig.add(b);
+    run_captured(G, "bwd" + std::to_string(control), sig, [&]() {
+        if (G.lame_on) ck(cudaMemsetAsync(G.glame->p, 0, G.glame->bytes, s), "memset");
+        if (k == 1) {
+            for (int i = L - 2; i >= control; --i) {
+                Layer& la = G.layers[i];
+                step_backward<R>(G, c, *la.pc, *G.layers[i + 1].pc, la.grid, la.trust, s);
+            }
+            return;
+        }
+        backward_segments<R>(G, c, control, L, k, s);
+    });
+}
+
+template <typename R>
+void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s)
+{
     int hi = L - 1;
     while (hi > control) {
         const int lo = ((hi - 1) / k) * k;
@@ -1670,6 +1856,15 @@ int mpm_profile_query(int kernel, long long* launches, double* total_ms)
 const char* mpm_kernel_name(int kernel) { return (kernel >= 0 && kernel < K_COUNT) ? k_names[kernel] : ""; }
 
 long long mpm_launch_count(void) { return g_prof.launches; }
+
+int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on)
+{
+    return guard([&] {
+        check_cg(cg);
+        cg->g.graphs_on = on != 0;
+        if (!on) cg->g.caps.clear();
+    });
+}
 
 int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on)
 {

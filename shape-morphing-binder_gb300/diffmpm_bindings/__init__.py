@@ -397,6 +397,10 @@ class CompGraph:
         ptr = getattr(stream, "cuda_stream", stream)
         check(lib.mpm_compgraph_set_stream(self._h, C.c_void_p(ptr) if ptr else None))
 
+    def use_graphs(self, on=True):
+        """Replay forward/backward passes as CUDA graphs (default on)."""
+        check(lib.mpm_compgraph_use_graphs(self._h, int(bool(on))))
+
     def enable_lame_grads(self, on=True):
         check(lib.mpm_compgraph_enable_lame_grads(self._h, int(bool(on))))
 

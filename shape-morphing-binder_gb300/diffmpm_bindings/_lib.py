@@ -96,6 +96,7 @@ _SIGS = {
     "mpm_compgraph_run_optimization": [_vp, C.POINTER(MpmOptInput)],
     "mpm_compgraph_active_nodes": [_vp, C.c_int, C.POINTER(C.c_ulonglong)],
     "mpm_compgraph_enable_lame_grads": [_vp, C.c_int],
+    "mpm_compgraph_use_graphs": [_vp, C.c_int],
     "mpm_compgraph_synchronize": [_vp],
     "mpm_profile_enable": [C.c_int],
     "mpm_profile_reset": [],

@@ -282,3 +282,60 @@ def test_autograd_rollout(dm):
             return float((((a - tgt) ** 2).mean() + 0.1 * ((b - torch.eye(3, dtype=torch.float64, device=dev)) ** 2).mean()))
     fd = (L(1e4 + eps) - L(1e4 - eps)) / (2 * eps)
     assert abs(float(E.grad) - fd) <= 1e-4 * abs(fd) + 1e-14, (float(E.grad), fd)
+
+
+@pytest.mark.parametrize("checkpoint_every", [1, 4])
+def test_graph_replay_matches_eager(dm, checkpoint_every):
+    """Forward/backward passes replayed from CUDA graphs equal eager passes;
+    changing a control (dFc of layer 0) re-records."""
+    s0, g, rng, _, _ = _case(11, G=12)
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.1, exact=True)
+    T = 8
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+
+    def run(cg):
+        out = []
+        for rep in range(5):  # eager, eager (allocations settle), record, replay, new control
+            if rep == 4:
+                cg.get_point_cloud(0).set("dFc", 0.02 * np.ones((s0.n, 3, 3)))
+            cg.compute_forward_pass(0, 0)
+            last = cg.get_point_cloud(T)
+            last.set("grad_x", seed_gx)
+            last.set("grad_v", np.zeros((s0.n, 3)))
+            last.set("grad_F", np.zeros((s0.n, 3, 3)))
+            last.set("grad_C", np.zeros((s0.n, 3, 3)))
+            cg.compute_backward_pass(0)
+            out.append((last.get("x", np.float64), cg.get_grad(0, "dFc", np.float64)))
+        return out
+
+    cg_a, ka = make_graph(dm, s0, g, prm, precision="fp64", adjoint="exact", layers=T + 1,
+                          checkpoint_every=checkpoint_every)
+    cg_b, kb = make_graph(dm, s0, g, prm, precision="fp64", adjoint="exact", layers=T + 1,
+                          checkpoint_every=checkpoint_every)
+    cg_b.use_graphs(False)
+    ra, rb = run(cg_a), run(cg_b)
+    for (xa, ga), (xb, gb) in zip(ra, rb):
+        assert rel_err(xa, xb) < 1e-12 and norm_err(ga, gb) < 1e-10
+    assert rel_err(ra[3][0], ra[2][0]) < 1e-12  # replay == recording run
+    assert rel_err(ra[4][0], ra[3][0]) > 1e-9  # the dFc change took effect
+
+
+def test_profiler_counts_graph_replays(dm):
+    s0, g, rng, _, _ = _case(12, G=10)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
+    T = 3
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=T + 1)
+    lib = dm._lib.lib
+    import ctypes as C
+    for _ in range(3):
+        cg.compute_forward_pass(0, 0)
+    lib.mpm_profile_reset()
+    lib.mpm_profile_enable(1)
+    try:
+        for _ in range(4):  # eager, record, replay, replay
+            cg.compute_forward_pass(0, 0)
+        cnt, ms = C.c_longlong(), C.c_double()
+        lib.mpm_profile_query(0, C.byref(cnt), C.byref(ms))  # p2g
+    finally:
+        lib.mpm_profile_enable(0)
+    assert cnt.value == 4 * T and ms.value > 0
