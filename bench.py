@@ -291,7 +291,7 @@ def run_ours(args, rank, world, device):
         "config": {"workload": w.name, "particles": n, "grid_nodes": list(w.dims), "dx": w.dx, "timesteps": T,
                    "instances": len(w.parts) if hasattr(w, "parts") else 1,
                    "checkpoint_every": w.checkpoint, "dt": w.dt, "density": round(w.rho, 3),
-                   "material": "fixed-corotated E=%g nu=%g" % (w.extra["E"], w.extra["nu"]),
+                   "material": "fixed-corotated E=%s nu=%s" % (w.extra["E"], w.extra["nu"]),
                    "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed steps (256 MiB write, outside the event brackets)",
                    "bench_step": "one rollout: forward T steps + loss gradient + backward T steps"},
