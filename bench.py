@@ -214,6 +214,7 @@ def run_ours(args, rank, world, device):
     cg.set_up_comp_graph(T + 1)
     stream = torch.cuda.current_stream(device)
     cg.set_stream(stream)
+    tuning = cg.autotune(steps=4) if not args.no_autotune else cg.get_tuning()
     tgt = torch.tensor(w.target, dtype=torch.float32, device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
 
@@ -294,7 +295,8 @@ def run_ours(args, rank, world, device):
                    "material": "fixed-corotated E=%s nu=%s" % (w.extra["E"], w.extra["nu"]),
                    "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed steps (256 MiB write, outside the event brackets)",
-                   "bench_step": "one rollout: forward T steps + loss gradient + backward T steps"},
+                   "bench_step": "one rollout: forward T steps + loss gradient + backward T steps",
+                   "tuning": tuning, "cuda_graphs": True},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
         "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
     }
@@ -473,6 +475,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="reduced workload for smoke runs")
     ap.add_argument("--timesteps", type=int, default=0, help="override the workload's timestep count")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -222,6 +222,15 @@ const char* mpm_kernel_name(int kernel);
 /* number of engine kernels launched since the library was loaded */
 long long mpm_launch_count(void);
 
+/* per-graph scatter strategy and node-tile budget (-1: library defaults,
+ * see mpm_set_scatter_mode / mpm_set_tile_nodes) */
+int mpm_compgraph_set_tuning(mpm_compgraph* cg, int tile_nodes, int scatter_mode);
+int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scatter_mode);
+/* No counterpart in the reference: time `steps`-step forward+backward passes
+ * of a scratch copy of this graph (layer 0's state) for each candidate
+ * scatter strategy and tile budget, keep the fastest for this graph and
+ * return it (best_ms: one timed forward+backward of the candidate) */
+int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms);
 /* record forward/backward passes as CUDA graphs and replay them (1 = on,
  * the default): a pass is recorded the second time it runs with the same
  * buffers and parameters and replayed from then on */

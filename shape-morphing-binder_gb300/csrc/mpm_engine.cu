@@ -550,6 +550,7 @@ struct Graph {
     };
     std::map<std::string, std::unique_ptr<Cap>> caps;
     bool graphs_on = true;
+    int tile_nodes = -1, scatter_mode = -1;  // tuning (-1: library defaults)
     // batch of independent instances (empty: one instance)
     std::vector<InstHost> inst;
     Buf inst_table;
@@ -579,6 +580,8 @@ struct Graph {
         c.kernel = opt.kernel;
         c.material = opt.material;
         c.exact = opt.adjoint == MPM_ADJ_EXACT;
+        c.tile_nodes = tile_nodes;
+        c.scatter_mode = scatter_mode;
         if (!inst.empty()) {
             c.inst = inst_table->p;
             c.ninst = (int)inst.size();
@@ -1856,6 +1859,90 @@ int mpm_profile_query(int kernel, long long* launches, double* total_ms)
 const char* mpm_kernel_name(int kernel) { return (kernel >= 0 && kernel < K_COUNT) ? k_names[kernel] : ""; }
 
 long long mpm_launch_count(void) { return g_prof.launches; }
+
+int mpm_compgraph_set_tuning(mpm_compgraph* cg, int tile_nodes, int scatter_mode)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (tile_nodes > 2816) fail(MPM_ERR_ARG, "tile nodes must be at most 2816");
+        if (scatter_mode > 1) fail(MPM_ERR_ARG, "scatter mode must be -1, 0 or 1");
+        cg->g.tile_nodes = tile_nodes;
+        cg->g.scatter_mode = scatter_mode;
+    });
+}
+
+int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scatter_mode)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (tile_nodes) *tile_nodes = cg->g.tile_nodes >= 0 ? cg->g.tile_nodes : g_tile_nodes;
+        if (scatter_mode) *scatter_mode = cg->g.scatter_mode >= 0 ? cg->g.scatter_mode : g_scatter_mode;
+    });
+}
+
+int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (steps < 1) fail(MPM_ERR_ARG, "steps must be positive");
+        if (!G.layers[0].pc || !G.layers[0].pc->have_state) fail(MPM_ERR_STATE, "layer 0 is not stored");
+        cudaStream_t s = G.stream;
+        // a scratch copy of the graph: layer 0's state, `steps` steps, full tape
+        Graph T;
+        T.prec = G.prec;
+        T.opt = G.opt;
+        T.opt.checkpoint_every = 1;
+        T.prm = G.prm;
+        T.geom = G.geom;
+        T.inst = G.inst;
+        T.inst_table = G.inst_table;
+        T.total_nodes = G.total_nodes;
+        T.stream = s;
+        T.base = clone_pc(*G.layers[0].pc, s, true);
+        T.base->grads.reset();
+        T.layers.resize(1);
+        T.layers[0].pc = T.base;
+        const int tiles[] = {0, 512, 1024, 2048};
+        double best = 1e300;
+        int bt = -1, bm = -1;
+        cudaEvent_t e0, e1;
+        ck(cudaEventCreate(&e0), "event");
+        ck(cudaEventCreate(&e1), "event");
+        with_prec(G.prec, [&](auto r) {
+            using R = decltype(r);
+            graph_set_up<R>(T, steps + 1);
+            for (int mode = (G.prec == MPM_FP32 ? 1 : 0); mode >= 0; --mode)
+                for (int tile : tiles) {
+                    if (G.prec != MPM_FP32 && tile != 0) continue;
+                    T.tile_nodes = tile;
+                    T.scatter_mode = mode;
+                    // eager, recorded, then timed replay (graphs) or third eager run
+                    for (int rep = 0; rep < 3; ++rep) {
+                        if (rep == 2) ck(cudaEventRecord(e0, s), "event");
+                        graph_forward<R>(T, 0);
+                        graph_backward<R>(T, 0);
+                        if (rep == 2) ck(cudaEventRecord(e1, s), "event");
+                    }
+                    ck(cudaEventSynchronize(e1), "event");
+                    float ms = 0;
+                    ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+                    if (ms < best) {
+                        best = ms;
+                        bt = tile;
+                        bm = mode;
+                    }
+                }
+        });
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        G.tile_nodes = bt;
+        G.scatter_mode = bm;
+        if (best_tile) *best_tile = bt;
+        if (best_mode) *best_mode = bm;
+        if (best_ms) *best_ms = best;
+    });
+}
 
 int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on)
 {

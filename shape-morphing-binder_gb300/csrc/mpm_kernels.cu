@@ -1469,12 +1469,14 @@ __global__ void k_nonfinite(int n, int k, long long ld, const R* __restrict__ y,
 }
 
 template <typename R>
-int tile_cap_for()
+int tile_cap_for(const StepCfg& c)
 {
     // shared float atomics are native; double tiles are not used (the plain
     // FP64 form scatters with global atomics)
-    return sizeof(R) == 4 ? g_tile_nodes : 0;
+    return sizeof(R) == 4 ? (c.tile_nodes >= 0 ? c.tile_nodes : g_tile_nodes) : 0;
 }
+
+inline int scatter_mode_of(const StepCfg& c) { return c.scatter_mode >= 0 ? c.scatter_mode : g_scatter_mode; }
 
 }  // namespace
 
@@ -1539,10 +1541,10 @@ void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
                 cudaStream_t s)
 {
     if (n <= 0) return;
-    const int cap = tile_cap_for<R>();
+    const int cap = tile_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
-        if (g_scatter_mode == 1) {
+        if (scatter_mode_of(c) == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 4);
             if (c.kernel == 0) {
                 ensure_smem(k_p2g_seg<4>, sm);
@@ -1581,10 +1583,10 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
                     const R* trust, R* adj, cudaStream_t s)
 {
     if (n <= 0) return;
-    const int cap = tile_cap_for<R>();
+    const int cap = tile_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
-        if (g_scatter_mode == 1) {
+        if (scatter_mode_of(c) == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 3);
             if (c.kernel == 0) {
                 ensure_smem(k_g2p_adj_seg<4>, sm);
@@ -1615,7 +1617,7 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
-    const int cap = tile_cap_for<R>();
+    const int cap = tile_cap_for<R>(c);
     const size_t sm = (size_t)cap * 2 * sizeof(float4);
     if (c.kernel == 0) {
         ensure_smem(k_p2g_adj<R, 4>, sm);

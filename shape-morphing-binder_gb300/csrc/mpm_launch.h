@@ -32,6 +32,9 @@ struct StepCfg {
     const void* inst = nullptr;
     int ninst = 0;
     long long total_nodes = 0;
+    // per-graph tuning (-1: the process-wide defaults below)
+    int tile_nodes = -1;
+    int scatter_mode = -1;
     long long nodes() const { return inst ? total_nodes : (long long)dims[0] * dims[1] * dims[2]; }
 };
 

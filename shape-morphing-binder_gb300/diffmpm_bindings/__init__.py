@@ -397,6 +397,21 @@ class CompGraph:
         ptr = getattr(stream, "cuda_stream", stream)
         check(lib.mpm_compgraph_set_stream(self._h, C.c_void_p(ptr) if ptr else None))
 
+    def autotune(self, steps: int = 4) -> dict:
+        """Pick the fastest scatter strategy / node-tile budget for this graph
+        by timing short forward+backward passes (additive)."""
+        t, m, ms = C.c_int(), C.c_int(), C.c_double()
+        check(lib.mpm_compgraph_autotune(self._h, int(steps), C.byref(t), C.byref(m), C.byref(ms)), "autotune")
+        return {"tile_nodes": t.value, "scatter_mode": m.value, "ms_per_pass": ms.value, "steps": int(steps)}
+
+    def set_tuning(self, tile_nodes=-1, scatter_mode=-1):
+        check(lib.mpm_compgraph_set_tuning(self._h, int(tile_nodes), int(scatter_mode)))
+
+    def get_tuning(self) -> dict:
+        t, m = C.c_int(), C.c_int()
+        check(lib.mpm_compgraph_get_tuning(self._h, C.byref(t), C.byref(m)))
+        return {"tile_nodes": t.value, "scatter_mode": m.value}
+
     def use_graphs(self, on=True):
         """Replay forward/backward passes as CUDA graphs (default on)."""
         check(lib.mpm_compgraph_use_graphs(self._h, int(bool(on))))

@@ -97,6 +97,9 @@ _SIGS = {
     "mpm_compgraph_active_nodes": [_vp, C.c_int, C.POINTER(C.c_ulonglong)],
     "mpm_compgraph_enable_lame_grads": [_vp, C.c_int],
     "mpm_compgraph_use_graphs": [_vp, C.c_int],
+    "mpm_compgraph_set_tuning": [_vp, C.c_int, C.c_int],
+    "mpm_compgraph_get_tuning": [_vp, _ip, _ip],
+    "mpm_compgraph_autotune": [_vp, C.c_int, _ip, _ip, _dp],
     "mpm_compgraph_synchronize": [_vp],
     "mpm_profile_enable": [C.c_int],
     "mpm_profile_reset": [],

@@ -339,3 +339,15 @@ def test_profiler_counts_graph_replays(dm):
     finally:
         lib.mpm_profile_enable(0)
     assert cnt.value == 4 * T and ms.value > 0
+
+
+def test_autotune_picks_a_valid_configuration(dm, orc):
+    s0, g, rng, _, _ = _case(13, G=12)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=3)
+    res = cg.autotune(steps=2)
+    assert res["tile_nodes"] in (0, 512, 1024, 2048) and res["scatter_mode"] in (0, 1) and res["ms_per_pass"] > 0
+    assert cg.get_tuning() == {"tile_nodes": res["tile_nodes"], "scatter_mode": res["scatter_mode"]}
+    cg.compute_forward_pass(0, 0)
+    want, _ = orc.forward_step(g, prm, s0)
+    assert rel_err(cg.get_point_cloud(1).get("x", np.float64), want.x) < 1e-6
