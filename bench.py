@@ -138,13 +138,13 @@ KERNEL_BYTES = {
 }
 
 
-def build_graph(dm, w, precision, checkpoint, adjoint="exact"):
+def build_graph(dm, w, precision, checkpoint, adjoint="exact", deterministic=False):
     dt = np.float64 if precision == "fp64" else np.float32
     pc = dm.PointCloud.from_arrays(w.x.astype(dt), v=w.v.astype(dt), F=w.F.astype(dt), m=w.m.astype(dt),
                                    vol=w.vol.astype(dt), lam=w.lam.astype(dt), mu=w.mu.astype(dt),
                                    precision=precision)
     grid = dm.Grid(*w.dims, w.dx, w.grid_min, precision=precision)
-    cg = dm.CompGraph(pc, grid, grid, adjoint=adjoint, checkpoint_every=checkpoint)
+    cg = dm.CompGraph(pc, grid, grid, adjoint=adjoint, checkpoint_every=checkpoint, deterministic=deterministic)
     cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
     return cg, (pc, grid)
 
@@ -177,7 +177,7 @@ class BatchWorkload:
         self.extra = {"E": "log-U[1e3,1e5]", "nu": "U[0.2,0.45]"}
 
 
-def build_batch_graph(dm, bw, precision):
+def build_batch_graph(dm, bw, precision, deterministic=False):
     dt = np.float64 if precision == "fp64" else np.float32
     pcs, grids = [], []
     for w in bw.parts:
@@ -185,7 +185,8 @@ def build_batch_graph(dm, bw, precision):
                                              vol=w.vol.astype(dt), lam=w.lam.astype(dt), mu=w.mu.astype(dt),
                                              precision=precision))
         grids.append(dm.Grid(*w.dims, w.dx, w.grid_min, precision=precision))
-    cg = dm.CompGraph.batch(pcs, grids, adjoint="exact", checkpoint_every=bw.checkpoint)
+    cg = dm.CompGraph.batch(pcs, grids, adjoint="exact", checkpoint_every=bw.checkpoint,
+                            deterministic=deterministic)
     cg.set_sim_params(dt=bw.dt, drag=bw.drag, smoothing=bw.smoothing)
     n_pad = len(cg.get_point_cloud(0))
     tgt = np.zeros((n_pad, 3))
@@ -203,13 +204,13 @@ def run_ours(args, rank, world, device):
     if args.workload == "batched":
         w = BatchWorkload(args.quick, args.timesteps)
         n, T = w.n, w.steps
-        cg, keep, tgt_np, n_pad = build_batch_graph(dm, w, "fp32")
+        cg, keep, tgt_np, n_pad = build_batch_graph(dm, w, "fp32", deterministic=args.deterministic)
         w.target = tgt_np
         args.no_e2e, args.no_fp64, args.no_cpu = True, True, True
     else:
         w = make_workload(args.workload, args.quick, args.timesteps)
         n, T = w.n, w.steps
-        cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
+        cg, keep = build_graph(dm, w, "fp32", w.checkpoint, deterministic=args.deterministic)
         n_pad = n
     cg.set_up_comp_graph(T + 1)
     stream = torch.cuda.current_stream(device)
@@ -296,7 +297,7 @@ def run_ours(args, rank, world, device):
                    "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed steps (256 MiB write, outside the event brackets)",
                    "bench_step": "one rollout: forward T steps + loss gradient + backward T steps",
-                   "tuning": tuning, "cuda_graphs": True},
+                   "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic)},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
         "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
     }
@@ -313,7 +314,8 @@ def run_e2e(torch, dm, args, w, device, keep):
     dL/dv0 and dL/dF0 out."""
     n, T = w.n, w.steps
     pc0, grid = keep
-    cg = dm.CompGraph(pc0, grid, grid, adjoint="exact", checkpoint_every=w.checkpoint)
+    cg = dm.CompGraph(pc0, grid, grid, adjoint="exact", checkpoint_every=w.checkpoint,
+                      deterministic=args.deterministic)
     cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
     cg.set_up_comp_graph(T + 1)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).pin_memory()  # noqa: E731
@@ -476,6 +478,8 @@ def main():
     ap.add_argument("--timesteps", type=int, default=0, help="override the workload's timestep count")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--deterministic", action="store_true",
+                    help="fixed-point node sums (bitwise reproducible passes)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

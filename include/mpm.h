@@ -90,6 +90,12 @@ typedef struct mpm_options {
     int material;         /* MPM_MAT_FCR (reference) or MPM_MAT_NEOHOOKEAN                  */
     int checkpoint_every; /* 1: keep every layer (reference tape); k > 1: keep every k-th
                              layer and recompute the others during the backward pass       */
+    int deterministic;    /* FP32 only, no counterpart in the reference (which sums nodes
+                             under `omp atomic`/`omp critical`, ForwardSimulation.cpp:26-80,
+                             BackPropagation.cpp:36-55): 1 = P2G, the G2P transpose and the
+                             loss's mass P2G sum node contributions in 64-bit fixed point,
+                             so results are bitwise reproducible run to run and a
+                             checkpointed backward recomputes the forward bit for bit      */
 } mpm_options;
 
 /* OptInput (bind.cpp:30-52) -- the fields run_optimization reads */
@@ -235,6 +241,11 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
  * the default): a pass is recorded the second time it runs with the same
  * buffers and parameters and replayed from then on */
 int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on);
+/* No counterpart in the reference: switch mpm_options.deterministic of an
+ * existing graph (MPM_ERR_ARG for FP64 graphs).  A pass whose node sums leave
+ * the fixed-point range (a non-finite or exploding state) fails with
+ * MPM_ERR_NONFINITE. */
+int mpm_compgraph_set_deterministic(mpm_compgraph* cg, int on);
 /* accumulate dL/dlambda and dL/dmu per particle over the next backward
  * passes; read them from the control layer's MPM_FIELD_GRAD_LAM/GRAD_MU */
 int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on);

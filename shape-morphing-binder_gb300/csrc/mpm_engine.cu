@@ -89,12 +89,9 @@ enum {
 };
 const char* k_names[K_COUNT] = {"p2g", "grid_update", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "mass_loss",
                                 "adam", "grad_norm", "aux"};
-// kernels each launcher issues (mass_loss: p2g, sums, nodes, gather)
-const int k_kernels[K_COUNT] = {1, 1, 1, 1, 1, 1, 4, 1, 1, 1};
 
 struct Prof {
     bool on = false;
-    long long launches = 0;
     struct Rec {
         int id;
         cudaEvent_t a, b;
@@ -139,7 +136,6 @@ struct KTimer {
     cudaEvent_t a = nullptr;
     KTimer(int id_, cudaStream_t s_) : id(id_), s(s_)
     {
-        g_prof.launches += k_kernels[id];
         if (g_prof.on) {
             a = g_prof.get();
             record(a);
@@ -551,6 +547,9 @@ struct Graph {
     std::map<std::string, std::unique_ptr<Cap>> caps;
     bool graphs_on = true;
     int tile_nodes = -1, scatter_mode = -1;  // tuning (-1: library defaults)
+    // deterministic scatters (opt.deterministic): fixed-point node
+    // accumulators, their control words and the adjoint scatter's inputs
+    Buf fix, fctl, fscr;
     // batch of independent instances (empty: one instance)
     std::vector<InstHost> inst;
     Buf inst_table;
@@ -582,10 +581,23 @@ struct Graph {
         c.exact = opt.adjoint == MPM_ADJ_EXACT;
         c.tile_nodes = tile_nodes;
         c.scatter_mode = scatter_mode;
+        double max_dx = geom.dx;
         if (!inst.empty()) {
             c.inst = inst_table->p;
             c.ninst = (int)inst.size();
             c.total_nodes = total_nodes;
+            for (const InstHost& h : inst) max_dx = std::max(max_dx, h.dx);
+        }
+        if (opt.deterministic && fix) {
+            c.fix = fix->p;
+            c.fix_ctl = fctl->as<unsigned>();
+            c.fix_scr = fscr->as<float>();
+            c.fix_count = (double)std::max(1, n());
+            // node momentum per unit of mass below 1024 cells per step: 256x
+            // above what any run inside the CFL limit produces
+            c.fix_speed = 1024.0 * max_dx / std::max(prm.dt, 1e-30);
+            // sum over axes of |x_i - x_p| < 2 dx per axis on the stencil
+            c.fix_reach = 6.0 * max_dx;
         }
         return c;
     }
@@ -628,13 +640,51 @@ Buf& ensure(Buf& b, size_t bytes, cudaStream_t s, bool zero)
     return b;
 }
 
+// Deterministic mode: allocate the fixed-point accumulators (zero) before
+// the pass's StepCfg is taken
+void prepare_fix(Graph& G)
+{
+    if (!G.opt.deterministic) return;
+    const long long nn = G.cfg().nodes();
+    ensure(G.fix, sizeof(long long) * 4 * nn, G.stream, true);
+    ensure(G.fctl, 4 * sizeof(unsigned), G.stream, true);
+    ensure(G.fscr, sizeof(float) * 12 * G.ld(), G.stream, false);
+}
+
+// start of a pass that scatters: clear the accumulators (robust against an
+// earlier pass that stopped between a scatter and its consumer) and find the
+// mass scale
+void begin_fix_pass(const Graph& G, const StepCfg& c, const PCData& d, cudaStream_t s)
+{
+    if (!c.det()) return;
+    ck(cudaMemsetAsync(G.fix->p, 0, G.fix->bytes, s), "memset");
+    launch_fix_prepare(c, d.n, d.ld, d.co->as<float>(), s);
+}
+
+// overflow flags of the fixed-point accumulators, read and cleared after a
+// synchronised API call
+void check_fix(Graph& G)
+{
+    if (!G.opt.deterministic || !G.fctl) return;
+    unsigned f = 0;
+    ck(cudaMemcpyAsync(&f, G.fctl->as<unsigned>() + 3, sizeof f, cudaMemcpyDeviceToHost, G.stream), "D2H");
+    ck(cudaStreamSynchronize(G.stream), "sync");
+    if (f) {
+        ck(cudaMemsetAsync(G.fctl->as<unsigned>() + 3, 0, sizeof f, G.stream), "memset");
+        ck(cudaStreamSynchronize(G.stream), "sync");
+        fail(MPM_ERR_NONFINITE,
+             "deterministic scatter: a node sum left the fixed-point range (non-finite or exploding state)");
+    }
+}
+
 // One forward step: layer i -> layer i+1 (ForwardSimulation.cpp:159-185)
 template <typename R>
 void step_forward(const StepCfg& c, PCData& a, PCData& b, Buf& grid, Buf& trust, cudaStream_t s)
 {
     const long long nn = c.nodes();
     ensure(grid, sizeof(R) * 4 * nn, s, false);
-    ck(cudaMemsetAsync(grid->p, 0, sizeof(R) * 4 * nn, s), "grid reset");
+    // the deterministic grid update writes every node
+    if (!c.det()) ck(cudaMemsetAsync(grid->p, 0, sizeof(R) * 4 * nn, s), "grid reset");
     const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
     {
         KTimer kt(K_P2G, s);
@@ -665,7 +715,7 @@ void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& 
     const long long nn = c.nodes();
     if (!grid) fail(MPM_ERR_STATE, "backward pass before the forward pass of this step");
     ensure(G.adj, sizeof(R) * 4 * nn, s, false);
-    ck(cudaMemsetAsync(G.adj->p, 0, sizeof(R) * 4 * nn, s), "adj reset");
+    if (!c.det()) ck(cudaMemsetAsync(G.adj->p, 0, sizeof(R) * 4 * nn, s), "adj reset");
     ensure_grads(a, s);
     ensure_grads(b, s);
     const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
@@ -768,7 +818,7 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
         }
     };
     if (c.exec && c.sig == sig.v) {
-        g_prof.launches += c.launches;
+        g_launches += c.launches;
         replay();
         return;
     }
@@ -789,7 +839,7 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
         body();  // eager: allocations and attribute setup happen here
         return;
     }
-    const long long l0 = g_prof.launches;
+    const long long l0 = g_launches;
     const size_t e0 = g_prof.pending.size();
     ck(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     g_prof.capturing = true;
@@ -809,7 +859,7 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
     cudaError_t e = cudaGraphInstantiate(&c.exec, graph, 0);
     cudaGraphDestroy(graph);
     ck(e, "cudaGraphInstantiate");
-    c.launches = g_prof.launches - l0;
+    c.launches = g_launches - l0;
     c.events.assign(g_prof.pending.begin() + e0, g_prof.pending.end());
     g_prof.pending.resize(e0);
     c.prof = g_prof.on;
@@ -824,6 +874,7 @@ void graph_forward(Graph& G, int start)
     const int L = (int)G.layers.size();
     if (start < 0 || start >= L) fail(MPM_ERR_RANGE, "start layer %d out of range [0, %d)", start, L);
     cudaStream_t s = G.stream;
+    prepare_fix(G);
     StepCfg c = G.cfg();
     const bool full = G.opt.checkpoint_every <= 1;
     if (!G.layers[start].pc || !G.layers[start].pc->have_state)
@@ -843,6 +894,7 @@ void graph_forward(Graph& G, int start)
     sig.add(G.ftrust);
     run_captured(G, "fwd" + std::to_string(start), sig, [&]() {
         PCData* cur = G.layers[start].pc.get();
+        begin_fix_pass(G, c, *cur, s);
         for (int i = start; i < L - 1; ++i) {
             PCData* nxt;
             if (G.stored(i + 1)) {
@@ -903,6 +955,7 @@ void graph_backward(Graph& G, int control)
     if (control < 0 || control >= L) fail(MPM_ERR_RANGE, "control layer %d out of range [0, %d)", control, L);
     cudaStream_t s = G.stream;
     inject_render_grads<R>(G);
+    prepare_fix(G);
     StepCfg c = G.cfg();
     const int k = std::max(1, G.opt.checkpoint_every);
     if (G.lame_on) {
@@ -929,6 +982,7 @@ void graph_backward(Graph& G, int control)
     for (auto& b : G.strust) sig.add(b);
     run_captured(G, "bwd" + std::to_string(control), sig, [&]() {
         if (G.lame_on) ck(cudaMemsetAsync(G.glame->p, 0, G.glame->bytes, s), "memset");
+        begin_fix_pass(G, c, *G.layers[control].pc, s);
         if (k == 1) {
             for (int i = L - 2; i >= control; --i) {
                 Layer& la = G.layers[i];
@@ -985,11 +1039,12 @@ double graph_loss(Graph& G)
     PCData& last = *G.layers.back().pc;
     if (!last.have_state) fail(MPM_ERR_STATE, "last layer not stored");
     ensure_grads(last, s);
+    prepare_fix(G);
     StepCfg c = G.cfg();
     const long long nn = c.nodes();
     ensure(G.lgm, sizeof(R) * nn, s, false);
     ensure(G.ldm, sizeof(R) * nn, s, false);
-    ensure(G.acc, sizeof(double) * 8, s, true);
+    ensure(G.acc, sizeof(double) * kRedDoubles, s, true);
     {
         KTimer kt(K_LOSS, s);
         launch_loss<R>(c, last.n, last.ld, last.st->as<R>(), last.co->as<R>(), G.target->nodes->as<R>(),
@@ -1007,7 +1062,7 @@ double graph_grad_norm(Graph& G, int layer)
 {
     PCData& d = *G.layers.at(layer).pc;
     cudaStream_t s = G.stream;
-    ensure(G.acc, sizeof(double) * 8, s, true);
+    ensure(G.acc, sizeof(double) * kRedDoubles, s, true);
     if (!d.grads) return 0.0;
     const R* g = d.gctl ? d.gctl->as<R>() : d.grads->as<R>() + ST_F * d.ld;
     {
@@ -1243,6 +1298,7 @@ void mpm_default_options(mpm_options* o)
     o->kernel = MPM_KERNEL_CUBIC;
     o->material = MPM_MAT_FCR;
     o->checkpoint_every = 1;
+    o->deterministic = 0;
 }
 
 void mpm_set_verbose(int v) { g_verbose = v; }
@@ -1451,6 +1507,7 @@ int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_gri
         mpm_default_params(&G.prm);
         G.prec = pc->d->prec;
         if (G.opt.precision != G.prec) fail(MPM_ERR_ARG, "options.precision differs from the PointCloud's");
+        if (G.opt.deterministic && G.prec != MPM_FP32) fail(MPM_ERR_ARG, "deterministic scatters are an FP32 option");
         if (grid->d->prec != G.prec) fail(MPM_ERR_ARG, "grid precision differs from the PointCloud's");
         ck(cudaStreamCreateWithFlags(&G.own, cudaStreamNonBlocking), "cudaStreamCreate");
         G.stream = G.own;
@@ -1488,6 +1545,7 @@ int mpm_compgraph_create_batch(const mpm_pointcloud* const* pcs, const mpm_grid*
         mpm_default_params(&G.prm);
         G.prec = pcs[0]->d->prec;
         if (G.opt.precision != G.prec) fail(MPM_ERR_ARG, "options.precision differs from the PointClouds'");
+        if (G.opt.deterministic && G.prec != MPM_FP32) fail(MPM_ERR_ARG, "deterministic scatters are an FP32 option");
         const long long B = 256;  // particle ranges start at multiples of the kernels' block size
         long long poff = 0, goff = 0;
         G.inst.resize(count);
@@ -1641,6 +1699,7 @@ int mpm_compgraph_forward(mpm_compgraph* cg, int start_layer, int episode)
         check_cg(cg);
         with_prec(cg->g.prec, [&](auto r) { graph_forward<decltype(r)>(cg->g, start_layer); });
         ck(cudaStreamSynchronize(cg->g.stream), "forward");
+        check_fix(cg->g);
     });
 }
 
@@ -1650,6 +1709,7 @@ int mpm_compgraph_backward(mpm_compgraph* cg, int control_layer)
         check_cg(cg);
         with_prec(cg->g.prec, [&](auto r) { graph_backward<decltype(r)>(cg->g, control_layer); });
         ck(cudaStreamSynchronize(cg->g.stream), "backward");
+        check_fix(cg->g);
     });
 }
 
@@ -1659,6 +1719,7 @@ int mpm_compgraph_mass_loss(mpm_compgraph* cg, double* loss)
         check_cg(cg);
         if (!loss) fail(MPM_ERR_ARG, "null output");
         with_prec(cg->g.prec, [&](auto r) { *loss = graph_loss<decltype(r)>(cg->g); });
+        check_fix(cg->g);
     });
 }
 
@@ -1793,6 +1854,7 @@ int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int t, int max_gd,
         check_cg(cg);
         with_prec(cg->g.prec, [&](auto r) { graph_optimize_single<decltype(r)>(cg->g, t, max_gd, episode, alpha, max_ls); });
         ck(cudaStreamSynchronize(cg->g.stream), "optimize");
+        check_fix(cg->g);
     });
 }
 
@@ -1804,6 +1866,7 @@ int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt)
         if (opt->num_timesteps < 1) fail(MPM_ERR_ARG, "num_timesteps must be positive");
         with_prec(cg->g.prec, [&](auto r) { graph_run_optimization<decltype(r)>(cg->g, *opt); });
         ck(cudaStreamSynchronize(cg->g.stream), "run_optimization");
+        check_fix(cg->g);
     });
 }
 
@@ -1858,7 +1921,7 @@ int mpm_profile_query(int kernel, long long* launches, double* total_ms)
 
 const char* mpm_kernel_name(int kernel) { return (kernel >= 0 && kernel < K_COUNT) ? k_names[kernel] : ""; }
 
-long long mpm_launch_count(void) { return g_prof.launches; }
+long long mpm_launch_count(void) { return g_launches; }
 
 int mpm_compgraph_set_tuning(mpm_compgraph* cg, int tile_nodes, int scatter_mode)
 {
@@ -1915,6 +1978,7 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
             for (int mode = (G.prec == MPM_FP32 ? 1 : 0); mode >= 0; --mode)
                 for (int tile : tiles) {
                     if (G.prec != MPM_FP32 && tile != 0) continue;
+                    if (G.opt.deterministic && mode != 1) continue;  // the fixed-point scatter is segmented
                     T.tile_nodes = tile;
                     T.scatter_mode = mode;
                     // eager, recorded, then timed replay (graphs) or third eager run
@@ -1950,6 +2014,15 @@ int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on)
         check_cg(cg);
         cg->g.graphs_on = on != 0;
         if (!on) cg->g.caps.clear();
+    });
+}
+
+int mpm_compgraph_set_deterministic(mpm_compgraph* cg, int on)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (on && cg->g.prec != MPM_FP32) fail(MPM_ERR_ARG, "deterministic scatters are an FP32 option");
+        cg->g.opt.deterministic = on != 0;
     });
 }
 

@@ -35,6 +35,7 @@ namespace mpm {
 
 int g_tile_nodes = 2048;
 int g_scatter_mode = 1;
+long long g_launches = 0;
 
 namespace {
 
@@ -113,6 +114,9 @@ MPM_D void bind_instance(KP<R>& kp, int& n_end, long long& goff)
 }
 
 inline int nblocks(long long n, int t = kThreads) { return (int)((n + t - 1) / t); }
+
+// every kernel launch of the launchers below is counted (host side)
+inline void counted() { ++g_launches; }
 
 // select a[i] from a small register array without dynamic indexing
 template <typename R, int K>
@@ -302,18 +306,72 @@ MPM_D void walk_rotated(const Stencil<R, K>& st, Fn&& f)
 
 constexpr int kRec = 40;  // u0[3], m, A[9], pad[3], w[3][K<=4], g[3][K<=4]
 
-inline size_t seg_smem_bytes(int CH, int tile_cap, int NC)
+inline size_t seg_smem_bytes(int CH, int tile_cap, int NC, bool det = false)
 {
-    return (size_t)CH * kRec * 4 + (size_t)tile_cap * NC * 4;
+    return (size_t)CH * kRec * 4 + (size_t)tile_cap * NC * (det ? 8 : 4);
 }
 
-template <int K, int NC>
+// Deterministic accumulation.  A value y is added to a node as the integer
+// round(y * 2^e) (two's complement in 64 bits); integer addition is
+// associative, so the node sum does not depend on the order in which blocks,
+// warps and cell groups deliver their contributions.  e is chosen per launch
+// from a bound B on the sum of |contributions| of the launch so that
+// B * 2^e < 2^62: no partial sum can wrap.  Resolution 2^-e = B * 2^-62 is
+// far below FP32 rounding of the node values for any realistic particle
+// count (2^21 particles leave 41 bits below the largest contribution).
+struct FixArgs {
+    unsigned long long* acc;  // 4 per node
+    unsigned* ctl;            // see StepCfg::fix_ctl
+    float count, speed, reach;
+};
+
+FixArgs make_fix(const StepCfg& c)
+{
+    FixArgs f;
+    f.acc = static_cast<unsigned long long*>(c.fix);
+    f.ctl = c.fix_ctl;
+    f.count = (float)c.fix_count;
+    f.speed = (float)c.fix_speed;
+    f.reach = (float)c.fix_reach;
+    return f;
+}
+
+// 2^e for -126 <= e <= 127, from the bit pattern
+MPM_D float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// e with bound * 2^e < 2^62 (bound < 2^(E+1) for the binary exponent E of
+// bound), clamped to +-120; 0 for a zero or NaN bound
+MPM_D int fix_exponent(float bound)
+{
+    if (!(bound > 0.f)) return 0;
+    const int E = (int)((__float_as_uint(bound) >> 23) & 0xFF) - 127;
+    return max(-120, min(120, 61 - E));
+}
+
+MPM_D float fix_mass_bound(const FixArgs& f) { return f.count * __uint_as_float(f.ctl[0]); }
+MPM_D float fix_adj_bound(const FixArgs& f)
+{
+    return f.count * (__uint_as_float(f.ctl[1]) + f.reach * __uint_as_float(f.ctl[2]));
+}
+
+// y * 2^e rounded to an integer; flags values at or beyond 2^61 (and NaN)
+MPM_D unsigned long long to_fix(float y, float scale, bool& ovf)
+{
+    const float z = y * scale;
+    ovf |= !(fabsf(z) < 0x1p61f);
+    return (unsigned long long)__float2ll_rn(z);
+}
+
+template <int K, int NC, bool DET = false>
 __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float, K>& st, const float* u0, float m,
-                            const float* A, float* __restrict__ grid, int tile_cap, unsigned char* smem)
+                            const float* A, float* __restrict__ grid, int tile_cap, unsigned char* smem,
+                            const FixArgs* fx = nullptr, const float* scale = nullptr)
 {
     const int CH = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     float* recs = reinterpret_cast<float*>(smem);
     float* tilebuf = recs + (size_t)CH * kRec;
+    unsigned long long* tilefix = reinterpret_cast<unsigned long long*>(tilebuf);
+    bool ovf = false;
     __shared__ int box[6];
     // 1. this lane's record, the block's bounding box of stencil bases
     if (t < 3) box[t] = INT_MAX;
@@ -368,7 +426,11 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
             e1 = (int)x1;
             e2 = (int)x2;
             vol = (int)(x0 * x1 * x2);
-            for (int i = t; i < NC * vol; i += CH) tilebuf[i] = 0.f;
+            if constexpr (DET) {
+                for (int i = t; i < NC * vol; i += CH) tilefix[i] = 0ull;
+            } else {
+                for (int i = t; i < NC * vol; i += CH) tilebuf[i] = 0.f;
+            }
         }
     }
     __syncthreads();
@@ -425,7 +487,19 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
                 if (h == 1 && !has1) break;
                 const float* acc = h == 0 ? acc0 : acc1;
                 const int i = i0 + (h == 0 ? a0 : a1), j = j0 + bb, k = k0 + cc;
-                if (tile) {
+                if constexpr (DET) {
+                    if (tile) {
+                        const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            if (acc[q] != 0.f) atomicAdd(&tilefix[q * vol + idx], to_fix(acc[q], scale[q], ovf));
+                    } else if (in_grid(kp, i, j, k)) {
+                        const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            if (acc[q] != 0.f) atomicAdd(&fx->acc[nd * 4 + q], to_fix(acc[q], scale[q], ovf));
+                    }
+                } else if (tile) {
                     const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
 #pragma unroll
                     for (int q = 0; q < NC; ++q)
@@ -441,6 +515,30 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
     }
     __syncthreads();
     // 5. flush the tile
+    if constexpr (DET) {
+        if (__any_sync(0xffffffffu, ovf) && lane == 0) atomicOr(&fx->ctl[3], 1u);
+        if (tile) {
+            for (int u = t; u < vol; u += CH) {
+                unsigned long long v[NC];
+                bool any = false;
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    v[q] = tilefix[q * vol + u];
+                    any |= v[q] != 0ull;
+                }
+                if (!any) continue;
+                const int kk = u % e2, rr = u / e2;
+                const int jj = rr % e1, ii = rr / e1;
+                const int i = b0 + ii, j = b1 + jj, k = b2 + kk;
+                if (!in_grid(kp, i, j, k)) continue;
+                const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+                for (int q = 0; q < NC; ++q)
+                    if (v[q] != 0ull) atomicAdd(&fx->acc[nd * 4 + q], v[q]);
+            }
+        }
+        return;
+    }
     if (tile) {
         for (int u = t; u < vol; u += CH) {
             float v[NC];
@@ -853,16 +951,17 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj(KP<R> kp, int n, long long
     sc.flush(kp, adj);
 }
 
-// P_op_1 + P2G with the segmented scatter (FP32 path)
-template <int K>
+// P_op_1 + P2G with the segmented scatter (FP32 path); DET: fixed-point sums
+template <int K, bool DET>
 __global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<float> kp, int n, long long ld, const float* __restrict__ st,
                                                        const float* __restrict__ dfc, const float* __restrict__ co,
-                                                       float* __restrict__ grid, int tile_cap)
+                                                       float* __restrict__ grid, int tile_cap, FixArgs fx)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     long long goff;
     bind_instance(kp, n, goff);
-    grid += goff * 4;
+    if constexpr (DET) fx.acc += goff * 4;
+    else grid += goff * 4;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = p < n;
     Stencil<float, K> sten;
@@ -888,7 +987,53 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<flo
         for (int a = 0; a < 3; ++a) mv[a] = mass * v[a] * kp.dragf;
         make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
     }
-    seg_scatter<K, 4>(kp, valid, sten, mv, mass, A, grid, tile_cap, smem);
+    if constexpr (DET) {
+        const float bm = fix_mass_bound(fx);
+        const float sp = pow2f(fix_exponent(bm * fx.speed)), sm = pow2f(fix_exponent(bm));
+        const float scale[4] = {sp, sp, sp, sm};
+        seg_scatter<K, 4, true>(kp, valid, sten, mv, mass, A, grid, tile_cap, smem, &fx, scale);
+    } else {
+        seg_scatter<K, 4>(kp, valid, sten, mv, mass, A, grid, tile_cap, smem);
+    }
+}
+
+// Deterministic mode: the node sums of P2G (fixed point) -> mass clamp +
+// G_op, as k_grid_update; clears the accumulators for the next step
+__global__ void k_grid_update_fix(KP<float> kp, long long nn, FixArgs fx, float* __restrict__ grid)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const float bm = fix_mass_bound(fx);
+    const float ip = pow2f(-fix_exponent(bm * fx.speed)), im = pow2f(-fix_exponent(bm));
+    longlong2* a = reinterpret_cast<longlong2*>(fx.acc + 4 * i);
+    const longlong2 q01 = a[0], q23 = a[1];
+    if ((q01.x | q01.y | q23.x | q23.y) != 0) {  // most nodes are empty: leave their zeros
+        a[0] = make_longlong2(0, 0);
+        a[1] = make_longlong2(0, 0);
+    }
+    const long long lim = 1ll << 62;
+    if (q01.x >= lim || q01.x <= -lim || q01.y >= lim || q01.y <= -lim || q23.x >= lim || q23.x <= -lim ||
+        q23.y >= lim || q23.y <= -lim)
+        atomicOr(&fx.ctl[3], 2u);
+    float m = __ll2float_rn(q23.y) * im;
+    if (m < 0.f) m = 0.f;
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    if (m > 1e-12f) {
+        v0 = __ll2float_rn(q01.x) * ip / m + kp.dtf[0];
+        v1 = __ll2float_rn(q01.y) * ip / m + kp.dtf[1];
+        v2 = __ll2float_rn(q23.x) * ip / m + kp.dtf[2];
+    }
+    reinterpret_cast<float4*>(grid)[i] = make_float4(v0, v1, v2, m);
+}
+
+// largest particle mass -> fix_ctl[0] (bits of a non-negative float order
+// like the floats)
+__global__ void k_fix_mass_max(int n, long long ld, const float* __restrict__ co, unsigned* ctl)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const float m = p < n ? fabsf(co[CO_M * ld + p]) : 0.f;
+    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(m == m ? m : 0.f));
+    if ((threadIdx.x & 31) == 0 && b) atomicMax(&ctl[0], b);
 }
 
 // P_op_2^T + G2P^T with the segmented scatter (FP32 path)
@@ -920,6 +1065,105 @@ __global__ void __launch_bounds__(kThreads) k_g2p_adj_seg(KP<float> kp, int n, l
         make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
     }
     seg_scatter<K, 3>(kp, valid, sten, vb, 0.f, CC, adj, tile_cap, smem);
+}
+
+// Deterministic mode, first half of P_op_2^T + G2P^T: the scatter inputs
+// (dL/dv_next, C0 dL/dC_next) of every particle into 12 scratch planes and
+// their largest magnitudes into fix_ctl[1], fix_ctl[2] (they set the
+// fixed-point scale of the scatter)
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_g2p_adj_prep(KP<float> kp, int n, long long ld,
+                                                            const float* __restrict__ st, const float* __restrict__ dfc,
+                                                            const float* __restrict__ st1, const float* __restrict__ g1,
+                                                            const float* __restrict__ trust, FixArgs fx,
+                                                            float* __restrict__ scr)
+{
+    long long goff;
+    bind_instance(kp, n, goff);
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    float vmx = 0.f, cmx = 0.f;
+    if (p < n) {
+        float F[9], Ft[9];
+        load_Ft(st, dfc, ld, p, F, Ft);
+        PostAdj<float> o;
+        post_adjoint(kp, ld, p, Ft, st1, g1, trust, o);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            scr[(long long)a * ld + p] = o.vbar[a];
+            vmx = fmaxf(vmx, fabsf(o.vbar[a]));
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const float c = kp.C0 * o.Cbar[i];
+            scr[(long long)(3 + i) * ld + p] = c;
+            cmx = fmaxf(cmx, fabsf(c));
+        }
+    }
+    const unsigned a = __reduce_max_sync(0xffffffffu, __float_as_uint(vmx));
+    const unsigned b = __reduce_max_sync(0xffffffffu, __float_as_uint(cmx));
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicMax(&fx.ctl[1], a);
+        if (b) atomicMax(&fx.ctl[2], b);
+    }
+}
+
+// Deterministic mode, second half: the G2P^T scatter in fixed point
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_g2p_adj_fix(KP<float> kp, int n, long long ld,
+                                                           const float* __restrict__ st, const float* __restrict__ scr,
+                                                           FixArgs fx, int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    fx.acc += goff * 4;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    Stencil<float, K> sten;
+    float vb[3], CC[9];
+    if (valid) {
+        float x[3];
+        load_planes(st + ST_X * ld, ld, p, 3, x);
+        load_planes(scr, ld, p, 3, vb);
+        load_planes(scr + 3 * ld, ld, p, 9, CC);
+        make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    const float sa = pow2f(fix_exponent(fix_adj_bound(fx)));
+    const float scale[3] = {sa, sa, sa};
+    seg_scatter<K, 3, true>(kp, valid, sten, vb, 0.f, CC, nullptr, tile_cap, smem, &fx, scale);
+}
+
+// G_op^T (BackPropagation.cpp:59-72) reading the fixed-point dL/dv sums;
+// writes all four adjoint slots and clears the accumulators
+__global__ void k_grid_adj_fix(KP<float> kp, long long nn, const float* __restrict__ grid, FixArgs fx,
+                               float* __restrict__ adj)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const float inv = pow2f(-fix_exponent(fix_adj_bound(fx)));
+    longlong2* a = reinterpret_cast<longlong2*>(fx.acc + 4 * i);
+    const longlong2 q01 = a[0], q23 = a[1];
+    if ((q01.x | q01.y | q23.x | q23.y) != 0) {
+        a[0] = make_longlong2(0, 0);
+        a[1] = make_longlong2(0, 0);
+    }
+    const long long lim = 1ll << 62;
+    if (q01.x >= lim || q01.x <= -lim || q01.y >= lim || q01.y <= -lim || q23.x >= lim || q23.x <= -lim)
+        atomicOr(&fx.ctl[3], 2u);
+    const float d0 = __ll2float_rn(q01.x) * inv, d1 = __ll2float_rn(q01.y) * inv, d2 = __ll2float_rn(q23.x) * inv;
+    const float4 g = reinterpret_cast<const float4*>(grid)[i];
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (fabsf(g.w) > 1e-12f) {
+        float v0 = g.x, v1 = g.y, v2 = g.z;
+        if (kp.exact) {
+            v0 -= kp.dtf[0];
+            v1 -= kp.dtf[1];
+            v2 -= kp.dtf[2];
+        }
+        const float im = 1.f / g.w;
+        out = make_float4(d0 * im, d1 * im, d2 * im, -(v0 * d0 + v1 * d1 + v2 * d2) * im);
+    }
+    reinterpret_cast<float4*>(adj)[i] = out;
 }
 
 // G_op^T (BackPropagation.cpp:59-72)
@@ -1204,9 +1448,52 @@ __global__ void __launch_bounds__(kThreads) k_mass_p2g(KP<R> kp, int n, long lon
     });
 }
 
+// deterministic mode: the loss's mass P2G into the fixed-point slot 3
+template <int K>
+__global__ void __launch_bounds__(kThreads) k_mass_p2g_fix(KP<float> kp, int n, long long ld,
+                                                            const float* __restrict__ st, const float* __restrict__ co,
+                                                            FixArgs fx)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float x[3];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    const float m = co[CO_M * ld + p];
+    const float scale = pow2f(fix_exponent(fix_mass_bound(fx)));
+    Stencil<float, K> sn;
+    make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    bool ovf = false;
+    walk_rotated<float, K>(sn, [&](int i, int j, int k, float w, float, float, float) {
+        if (in_grid(kp, i, j, k)) atomicAdd(&fx.acc[node_of(kp, i, j, k) * 4 + 3], to_fix(w * m, scale, ovf));
+    });
+    if (ovf) atomicOr(&fx.ctl[3], 1u);
+}
+
+__global__ void k_fix_mass_out(long long nn, FixArgs fx, float* __restrict__ gm)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const long long q = (long long)fx.acc[4 * i + 3];
+    if (q) fx.acc[4 * i + 3] = 0ull;
+    gm[i] = __ll2float_rn(q) * pow2f(-fix_exponent(fix_mass_bound(fx)));
+}
+
+// Deterministic reductions: each block writes its partial sum(s) to
+// parts[block * stride + column]; k_sum_parts adds them up in a fixed order
+// (one warp per column, lane-strided, then a fixed shuffle tree).
+__global__ void k_sum_parts(const double* __restrict__ parts, int count, int stride, int cols, double* out)
+{
+    const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (c >= cols) return;
+    double s = 0;
+    for (int j = lane; j < count; j += 32) s += parts[(long long)j * stride + c];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[c] = s;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_loss_sums(long long nn, const R* __restrict__ gm,
-                                                         const R* __restrict__ tm, double* acc)
+                                                         const R* __restrict__ tm, double* parts)
 {
     __shared__ double red[32];
     double a = 0, b = 0;
@@ -1217,8 +1504,8 @@ __global__ void __launch_bounds__(kThreads) k_loss_sums(long long nn, const R* _
     a = block_sum<R>(a, red);
     b = block_sum<R>(b, red);
     if (threadIdx.x == 0) {
-        atomicAdd(&acc[0], a);
-        atomicAdd(&acc[1], b);
+        parts[2 * blockIdx.x] = a;
+        parts[2 * blockIdx.x + 1] = b;
     }
 }
 
@@ -1226,7 +1513,7 @@ __global__ void __launch_bounds__(kThreads) k_loss_sums(long long nn, const R* _
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_loss_nodes(long long nn, const R* __restrict__ gm,
                                                           const R* __restrict__ tm, R* __restrict__ dLdm,
-                                                          double* acc)
+                                                          const double* acc, double* parts)
 {
     __shared__ double red[32];
     const double eps = 1e-4, min_mass = 1e-3, eps_s = 1e-6;
@@ -1249,8 +1536,8 @@ __global__ void __launch_bounds__(kThreads) k_loss_nodes(long long nn, const R* 
     loss = block_sum<R>(loss, red);
     gc = block_sum<R>(gc, red);
     if (threadIdx.x == 0) {
-        atomicAdd(&acc[2], loss);
-        atomicAdd(&acc[3], gc);
+        parts[2 * blockIdx.x] = loss;
+        parts[2 * blockIdx.x + 1] = gc;
     }
 }
 
@@ -1354,7 +1641,7 @@ __global__ void __launch_bounds__(kThreads) k_volumes(KP<R> kp, int n, long long
 
 template <typename R>
 __global__ void __launch_bounds__(kThreads) k_sumsq(int n, long long ld, const R* __restrict__ g, int planes,
-                                                     double* acc)
+                                                     double* parts)
 {
     __shared__ double red[32];
     double s = 0;
@@ -1364,7 +1651,7 @@ __global__ void __launch_bounds__(kThreads) k_sumsq(int n, long long ld, const R
             s += v * v;
         }
     s = block_sum<R>(s, red);
-    if (threadIdx.x == 0) atomicAdd(acc, s);
+    if (threadIdx.x == 0) parts[blockIdx.x] = s;
 }
 
 // Descend_Adam (PointCloud.cpp:83-147) with FP64 moments
@@ -1544,19 +1831,37 @@ void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
     const int cap = tile_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
+        if (c.det()) {
+            const FixArgs fx = make_fix(c);
+            const size_t sm = seg_smem_bytes(kThreads, cap, 4, true);
+            if (c.kernel == 0) {
+                ensure_smem(k_p2g_seg<4, true>, sm);
+                counted();
+                k_p2g_seg<4, true><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+            } else {
+                ensure_smem(k_p2g_seg<3, true>, sm);
+                counted();
+                k_p2g_seg<3, true><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+            }
+            return;
+        }
         if (scatter_mode_of(c) == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 4);
+            const FixArgs fx{};
             if (c.kernel == 0) {
-                ensure_smem(k_p2g_seg<4>, sm);
-                k_p2g_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+                ensure_smem(k_p2g_seg<4, false>, sm);
+                counted();
+                k_p2g_seg<4, false><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             } else {
-                ensure_smem(k_p2g_seg<3>, sm);
-                k_p2g_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+                ensure_smem(k_p2g_seg<3, false>, sm);
+                counted();
+                k_p2g_seg<3, false><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             }
             return;
         }
     }
     const size_t sm = (size_t)cap * 4 * sizeof(R);
+    counted();
     if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
     else k_p2g<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
 }
@@ -1565,6 +1870,14 @@ template <typename R>
 void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s)
 {
     const long long nn = c.nodes();
+    if constexpr (sizeof(R) == 4) {
+        if (c.det()) {
+            counted();
+            k_grid_update_fix<<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, make_fix(c), grid);
+            return;
+        }
+    }
+    counted();
     k_grid_update<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid);
 }
 
@@ -1574,6 +1887,7 @@ void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
+    counted();
     if (c.kernel == 0) k_g2p<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
     else k_g2p<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
 }
@@ -1586,19 +1900,42 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
     const int cap = tile_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
+        if (c.det()) {
+            // inputs of the scatter and their bound first, then the scatter
+            const FixArgs fx = make_fix(c);
+            cudaMemsetAsync(c.fix_ctl + 1, 0, 2 * sizeof(unsigned), s);
+            const size_t sm = seg_smem_bytes(kThreads, cap, 3, true);
+            if (c.kernel == 0) {
+                counted();
+                k_g2p_adj_prep<4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
+                ensure_smem(k_g2p_adj_fix<4>, sm);
+                counted();
+                k_g2p_adj_fix<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
+            } else {
+                counted();
+                k_g2p_adj_prep<3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
+                ensure_smem(k_g2p_adj_fix<3>, sm);
+                counted();
+                k_g2p_adj_fix<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
+            }
+            return;
+        }
         if (scatter_mode_of(c) == 1) {
             const size_t sm = seg_smem_bytes(kThreads, cap, 3);
             if (c.kernel == 0) {
                 ensure_smem(k_g2p_adj_seg<4>, sm);
+                counted();
                 k_g2p_adj_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             } else {
                 ensure_smem(k_g2p_adj_seg<3>, sm);
+                counted();
                 k_g2p_adj_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             }
             return;
         }
     }
     const size_t sm = (size_t)cap * 3 * sizeof(R);
+    counted();
     if (c.kernel == 0) k_g2p_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
     else k_g2p_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
 }
@@ -1607,6 +1944,14 @@ template <typename R>
 void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s)
 {
     const long long nn = c.nodes();
+    if constexpr (sizeof(R) == 4) {
+        if (c.det()) {
+            counted();
+            k_grid_adj_fix<<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, make_fix(c), adj);
+            return;
+        }
+    }
+    counted();
     k_grid_adj<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, adj);
 }
 
@@ -1621,10 +1966,12 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
     const size_t sm = (size_t)cap * 2 * sizeof(float4);
     if (c.kernel == 0) {
         ensure_smem(k_p2g_adj<R, 4>, sm);
+        counted();
         k_p2g_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
                                                           glam, gmu, cap);
     } else {
         ensure_smem(k_p2g_adj<R, 3>, sm);
+        counted();
         k_p2g_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
                                                           glam, gmu, cap);
     }
@@ -1636,16 +1983,41 @@ void launch_loss(const StepCfg& c, int n, long long ld, const R* st, const R* co
 {
     const long long nn = c.nodes();
     auto kp = make_kp<R>(c);
-    cudaMemsetAsync(gm, 0, sizeof(R) * nn, s);
-    cudaMemsetAsync(acc, 0, sizeof(double) * 4, s);
-    if (n > 0) {
-        if (c.kernel == 0) k_mass_p2g<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
-        else k_mass_p2g<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
+    bool fixed = false;
+    if constexpr (sizeof(R) == 4) {
+        if (c.det()) {
+            const FixArgs fx = make_fix(c);
+            launch_fix_prepare(c, n, ld, co, s);
+            if (n > 0) {
+                counted();
+                if (c.kernel == 0) k_mass_p2g_fix<4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, fx);
+                else k_mass_p2g_fix<3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, fx);
+            }
+            counted();
+            k_fix_mass_out<<<nblocks(nn), kThreads, 0, s>>>(nn, fx, gm);
+            fixed = true;
+        }
     }
-    const int nb = (int)std::min<long long>(nblocks(nn), 1184);
-    k_loss_sums<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, acc);
-    k_loss_nodes<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, dLdm, acc);
+    if (!fixed) {
+        cudaMemsetAsync(gm, 0, sizeof(R) * nn, s);
+        if (n > 0) {
+            counted();
+            if (c.kernel == 0) k_mass_p2g<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
+            else k_mass_p2g<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, gm);
+        }
+    }
+    const int nb = (int)std::min<long long>(nblocks(nn), kRedParts);
+    double* parts = acc + 8;
+    counted();
+    k_loss_sums<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, parts);
+    counted();
+    k_sum_parts<<<1, 64, 0, s>>>(parts, nb, 2, 2, acc);
+    counted();
+    k_loss_nodes<R><<<nb, kThreads, 0, s>>>(nn, gm, target_m, dLdm, acc, parts);
+    counted();
+    k_sum_parts<<<1, 64, 0, s>>>(parts, nb, 2, 2, acc + 2);
     if (n > 0) {
+        counted();
         if (c.kernel == 0) k_loss_grad<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, target_m, dLdm, acc, g);
         else k_loss_grad<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, target_m, dLdm, acc, g);
     }
@@ -1656,6 +2028,7 @@ void launch_p2g_plain(const StepCfg& c, int n, long long ld, const R* st, const 
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
+    counted();
     if (c.kernel == 0) k_p2g_plain<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
     else k_p2g_plain<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
 }
@@ -1665,6 +2038,7 @@ void launch_volumes(const StepCfg& c, int n, long long ld, const R* st, R* co, c
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
+    counted();
     if (c.kernel == 0) k_volumes<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
     else k_volumes<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, co, grid);
 }
@@ -1672,10 +2046,22 @@ void launch_volumes(const StepCfg& c, int n, long long ld, const R* st, R* co, c
 template <typename R>
 void launch_sumsq(int n, long long ld, const R* g, int plane0, int planes, double* acc, cudaStream_t s)
 {
-    cudaMemsetAsync(acc, 0, sizeof(double), s);
-    if (n <= 0) return;
-    const int nb = std::min(nblocks(n), 1184);
-    k_sumsq<R><<<nb, kThreads, 0, s>>>(n, ld, g + (long long)plane0 * ld, planes, acc);
+    if (n <= 0) {
+        cudaMemsetAsync(acc, 0, sizeof(double), s);
+        return;
+    }
+    const int nb = std::min(nblocks(n), kRedParts);
+    counted();
+    k_sumsq<R><<<nb, kThreads, 0, s>>>(n, ld, g + (long long)plane0 * ld, planes, acc + 8);
+    counted();
+    k_sum_parts<<<1, 32, 0, s>>>(acc + 8, nb, 1, 1, acc);
+}
+
+void launch_fix_prepare(const StepCfg& c, int n, long long ld, const float* co, cudaStream_t s)
+{
+    cudaMemsetAsync(c.fix_ctl, 0, 3 * sizeof(unsigned), s);
+    counted();
+    if (n > 0) k_fix_mass_max<<<nblocks(n), kThreads, 0, s>>>(n, ld, co, c.fix_ctl);
 }
 
 template <typename R>
@@ -1684,6 +2070,7 @@ void launch_adam(int n, long long ld, const R* gF, R* dfc, double* mom, double* 
 {
     if (n <= 0) return;
     const double bc1 = 1.0 - pow(beta1, t), bc2 = 1.0 - pow(beta2, t);
+    counted();
     k_adam<R><<<nblocks(n), kThreads, 0, s>>>(n, ld, gF, dfc, mom, vec, vmax, alpha, inv_gn, beta1, beta2, eps, bc1,
                                                bc2);
 }
@@ -1692,6 +2079,7 @@ template <typename R, typename T>
 void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s)
 {
     if (n <= 0) return;
+    counted();
     k_aos_to_planes<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
 }
 
@@ -1699,6 +2087,7 @@ template <typename R, typename T>
 void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s)
 {
     if (n <= 0) return;
+    counted();
     k_planes_to_aos<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
 }
 
@@ -1706,6 +2095,7 @@ template <typename R>
 void launch_axpy_planes(int n, int k, long long ld, R alpha, const R* x, R* y, cudaStream_t s)
 {
     if (n <= 0) return;
+    counted();
     k_axpy_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, alpha, x, y);
 }
 
@@ -1713,6 +2103,7 @@ template <typename R>
 void launch_fill_planes(int n, int k, long long ld, R value, R* y, cudaStream_t s)
 {
     if (n <= 0) return;
+    counted();
     k_fill_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, value, y);
 }
 
@@ -1721,6 +2112,7 @@ void launch_count_active(const StepCfg& c, const R* grid, unsigned long long* ou
 {
     cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
     const long long nn = c.nodes();
+    counted();
     k_count_active<R><<<nblocks(nn), kThreads, 0, s>>>(nn, grid, out);
 }
 
@@ -1728,6 +2120,7 @@ template <typename R>
 void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStream_t s)
 {
     if (n <= 0) return;
+    counted();
     k_nonfinite<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, y, flag);
 }
 

@@ -35,8 +35,28 @@ struct StepCfg {
     // per-graph tuning (-1: the process-wide defaults below)
     int tile_nodes = -1;
     int scatter_mode = -1;
+    // Deterministic scatters (FP32 segmented path): node sums accumulate in
+    // 64-bit fixed point, so their value does not depend on the order of the
+    // atomics.  fix: 4 words per node, all zero between steps (the grid
+    // kernels that consume them clear them); fix_ctl: 4 words, [0] bits of
+    // the largest particle mass, [1] bits of the largest |dL/dv_next|,
+    // [2] bits of the largest |C0 dL/dC_next|, [3] overflow flags;
+    // fix_scr: 12 particle planes (the G2P transpose's scatter inputs).
+    // Scales are powers of two chosen so that every partial sum stays below
+    // 2^62: mass from count * max m, momentum from that times fix_speed,
+    // the adjoint from count * (max|dL/dv| + fix_reach * max|C0 dL/dC|).
+    void* fix = nullptr;
+    unsigned* fix_ctl = nullptr;
+    float* fix_scr = nullptr;
+    double fix_count = 0, fix_speed = 0, fix_reach = 0;
     long long nodes() const { return inst ? total_nodes : (long long)dims[0] * dims[1] * dims[2]; }
+    bool det() const { return fix != nullptr; }
 };
+
+// partial sums of the deterministic reductions live after the first 8
+// doubles of a reduction buffer: 8 + 2 * kRedParts doubles in all
+constexpr int kRedParts = 1184;
+constexpr size_t kRedDoubles = 8 + 2 * (size_t)kRedParts;
 
 // host mirror of one batch instance (converted to the kernels' table)
 struct InstHost {
@@ -54,6 +74,8 @@ extern int g_tile_nodes;
 // FP32 scatter strategy: 1 = segmented (warp per cell segment, lane per
 // node), 0 = per-particle scatter
 extern int g_scatter_mode;
+// kernels launched by the launchers below (host-side count)
+extern long long g_launches;
 
 template <typename R>
 void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
@@ -75,7 +97,8 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
                     cudaStream_t s);
 
 // mass loss (CompGraph.cpp:42-129).  target: a grid (4 scalars per node, mass
-// in slot 3); acc: 4 doubles (sum_c, sum_t, loss, sum g*c)
+// in slot 3); acc: kRedDoubles doubles, results in the first 4 (sum_c,
+// sum_t, loss, sum g*c), summed in a fixed order
 template <typename R>
 void launch_loss(const StepCfg& c, int n, long long ld, const R* st, const R* co, const R* target_m, R* gm, R* dLdm,
                  double* acc, R* g, cudaStream_t s);
@@ -87,6 +110,7 @@ template <typename R>
 void launch_volumes(const StepCfg& c, int n, long long ld, const R* st, R* co, const R* grid, cudaStream_t s);
 
 // Adam over one layer's control (PointCloud.cpp:83-147); sumsq of dL/dF
+// into acc[0] (acc: kRedDoubles doubles, summed in a fixed order)
 template <typename R>
 void launch_sumsq(int n, long long ld, const R* g, int plane0, int planes, double* acc, cudaStream_t s);
 template <typename R>
@@ -108,6 +132,10 @@ void launch_count_active(const StepCfg& c, const R* grid, unsigned long long* ou
 // non-finite check over planes; sets *flag = 1 on NaN/Inf
 template <typename R>
 void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStream_t s);
+
+// deterministic mode: clear fix_ctl[0..2] and store the largest particle
+// mass in fix_ctl[0] (start of every pass that scatters)
+void launch_fix_prepare(const StepCfg& c, int n, long long ld, const float* co, cudaStream_t s);
 
 // record the message mpm_last_error() returns on this host thread
 void set_last_error(const char* msg);

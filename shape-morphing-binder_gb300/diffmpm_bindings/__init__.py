@@ -294,11 +294,13 @@ class CompGraph:
     ``options`` (additive) selects precision ('fp32'/'fp64'), the adjoint
     ('reference' reproduces BackPropagation.cpp term for term, 'exact' is the
     true derivative), the kernel ('cubic'/'quadratic'), the material
-    ('fcr'/'neohookean') and checkpointing (keep every k-th layer).
+    ('fcr'/'neohookean'), checkpointing (keep every k-th layer) and
+    ``deterministic`` (FP32: node sums in 64-bit fixed point, bitwise
+    reproducible).
     """
 
     def __init__(self, point_cloud: PointCloud, grid: Grid, target_grid: Grid, *, adjoint="reference",
-                 kernel="cubic", material="fcr", checkpoint_every=1):
+                 kernel="cubic", material="fcr", checkpoint_every=1, deterministic=False):
         if point_cloud is None or grid is None:
             raise RuntimeError("PointCloud or Grid is null.")
         o = MpmOptions()
@@ -311,6 +313,7 @@ class CompGraph:
         o.material = {"fcr": MPM_MAT_FCR, "neohookean": MPM_MAT_NEOHOOKEAN}[material] \
             if isinstance(material, str) else int(material)
         o.checkpoint_every = int(checkpoint_every)
+        o.deterministic = int(bool(deterministic))
         h = C.c_void_p()
         check(lib.mpm_compgraph_create(point_cloud._h, grid._h, target_grid._h if target_grid is not None else None,
                                        C.byref(o), C.byref(h)), "CompGraph")
@@ -327,7 +330,7 @@ class CompGraph:
 
     @classmethod
     def batch(cls, point_clouds, grids, *, adjoint="reference", kernel="cubic", material="fcr",
-              checkpoint_every=1) -> "CompGraph":
+              checkpoint_every=1, deterministic=False) -> "CompGraph":
         """Independent instances advanced together in one launch per kernel
         (additive; BASELINE configuration 3).  ``instance_range(i)`` gives the
         slice of instance i in the concatenated layer arrays."""
@@ -340,6 +343,7 @@ class CompGraph:
         o.kernel = {"cubic": MPM_KERNEL_CUBIC, "quadratic": MPM_KERNEL_QUADRATIC}[kernel]
         o.material = {"fcr": MPM_MAT_FCR, "neohookean": MPM_MAT_NEOHOOKEAN}[material]
         o.checkpoint_every = int(checkpoint_every)
+        o.deterministic = int(bool(deterministic))
         k = len(point_clouds)
         pcs = (C.c_void_p * k)(*[p._h for p in point_clouds])
         gs = (C.c_void_p * k)(*[g._h for g in grids])
@@ -366,7 +370,11 @@ class CompGraph:
         o = MpmOptions()
         check(lib.mpm_compgraph_get_options(self._h, C.byref(o)))
         return dict(precision=o.precision, adjoint=o.adjoint, kernel=o.kernel, material=o.material,
-                    checkpoint_every=o.checkpoint_every)
+                    checkpoint_every=o.checkpoint_every, deterministic=bool(o.deterministic))
+
+    def set_deterministic(self, on=True):
+        """Fixed-point node sums (FP32 graphs): bitwise reproducible passes."""
+        check(lib.mpm_compgraph_set_deterministic(self._h, int(bool(on))))
 
     def get_sim_params(self) -> dict:
         p = MpmParams()

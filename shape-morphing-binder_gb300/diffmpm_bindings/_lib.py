@@ -33,7 +33,7 @@ class MpmParams(C.Structure):
 
 class MpmOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("adjoint", C.c_int), ("kernel", C.c_int), ("material", C.c_int),
-                ("checkpoint_every", C.c_int)]
+                ("checkpoint_every", C.c_int), ("deterministic", C.c_int)]
 
 
 class MpmOptInput(C.Structure):
@@ -98,6 +98,7 @@ _SIGS = {
     "mpm_compgraph_enable_lame_grads": [_vp, C.c_int],
     "mpm_compgraph_use_graphs": [_vp, C.c_int],
     "mpm_compgraph_set_tuning": [_vp, C.c_int, C.c_int],
+    "mpm_compgraph_set_deterministic": [_vp, C.c_int],
     "mpm_compgraph_get_tuning": [_vp, _ip, _ip],
     "mpm_compgraph_autotune": [_vp, C.c_int, _ip, _ip, _dp],
     "mpm_compgraph_synchronize": [_vp],

@@ -339,6 +339,10 @@ def test_profiler_counts_graph_replays(dm):
     finally:
         lib.mpm_profile_enable(0)
     assert cnt.value == 4 * T and ms.value > 0
+    # the launch counter counts kernels: P2G, grid update, G2P per step
+    n0 = lib.mpm_launch_count()
+    cg.compute_forward_pass(0, 0)
+    assert lib.mpm_launch_count() - n0 == 3 * T
 
 
 def test_autotune_picks_a_valid_configuration(dm, orc):
