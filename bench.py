@@ -308,6 +308,80 @@ def run_ours(args, rank, world, device):
     return line
 
 
+def run_morph(args, device):
+    """BASELINE configuration 5 end to end: a 500k-particle sphere morphed
+    towards targets displaced by seeded real spherical harmonics (l <= 4),
+    one episode per target.  Each episode is run_optimization
+    (OptimizeDefGradControlSequence) over 200 steps per pass, control stride
+    10 (20 control steps), lr 1e-2, 10 passes, FP64 Adam moments and the
+    deterministic fixed-point scatters; the next episode starts from the last
+    layer (promote_last_as_initial, as run.py does between episodes).
+    Timed on the host clock around each synchronous run_optimization call
+    (everything included: line-search forwards, loss read-backs).  --warmup
+    runs short episodes (one pass), --steps the timed episodes."""
+    import torch
+    import diffmpm_bindings as dm
+    from diffmpm_bindings import workloads as W
+    lib = dm._lib.lib
+    lib.mpm_set_verbose(0)
+    n_part = 50_000 if args.quick else 500_000
+    w0 = W.morph500k(n=n_part, episode=0)
+    n = w0.n
+    steps = args.timesteps or (40 if args.quick else 200)
+    passes = 2 if args.quick else 10
+    pc0 = dm.PointCloud.from_arrays(w0.x.astype(np.float32), v=w0.v.astype(np.float32), F=w0.F.astype(np.float32),
+                                    m=w0.m.astype(np.float32), vol=w0.vol.astype(np.float32),
+                                    lam=w0.lam.astype(np.float32), mu=w0.mu.astype(np.float32))
+    grid = dm.Grid(*w0.dims, w0.dx, w0.grid_min)
+    target = dm.Grid(*w0.dims, w0.dx, w0.grid_min)
+    cg = dm.CompGraph(pc0, grid, target, checkpoint_every=10, deterministic=True)
+    opt = dm.OptInput()
+    opt.num_timesteps, opt.control_stride, opt.max_gd_iters, opt.max_ls_iters = steps + 1, 10, 1, 4
+    opt.dt, opt.drag, opt.smoothing_factor = w0.dt, w0.drag, w0.smoothing
+    opt.initial_alpha, opt.gd_tol = 1e-2, 1e-4
+
+    def set_target(e):
+        we = W.morph500k(n=n_part, episode=e)
+        target.set_node_masses(np.zeros(target.num_nodes))
+        tpc = dm.PointCloud.from_arrays(we.target.astype(np.float32), m=we.m.astype(np.float32))
+        dm.p2g(tpc, target)
+
+    for e in range(args.warmup):
+        set_target(100 + e)
+        cg.run_optimization(opt, passes=1)
+    episodes = []
+    f0, b0 = dm.step_count()
+    total = 0.0
+    with Clocks(device.index if device.index is not None else 0) as clk:
+        for e in range(args.steps):
+            set_target(e)
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            cg.run_optimization(opt, passes=passes)
+            torch.cuda.synchronize(device)
+            dt_e = time.perf_counter() - t0
+            total += dt_e
+            h = cg.loss_history()
+            episodes.append({"episode": e, "seconds": round(dt_e, 3), "initial_loss": float(h[0]),
+                             "final_loss": float(h[-1]), "losses_evaluated": int(len(h))})
+            cg.promote_last_as_initial()
+    f1, b1 = dm.step_count()
+    psteps = n * ((f1 - f0) + (b1 - b0))
+    return {
+        "metric": "configuration-5 optimisation, particle-steps/s end to end", "value": round(psteps / total, 1),
+        "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "seconds_per_episode": round(total / max(1, args.steps), 3), "seconds_total": round(total, 3),
+        "higher_is_better": True, "dtype": "f32 (FP64-guarded stress, FP64 Adam moments)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "morph500k" if not args.quick else "morph50k", "particles": n,
+                   "grid_nodes": list(w0.dims), "dx": w0.dx, "timesteps_per_pass": steps, "control_stride": 10,
+                   "passes": passes, "episodes": args.steps, "lr": 1e-2, "max_line_search": 4,
+                   "checkpoint_every": 10, "deterministic": True, "adjoint": "reference",
+                   "target": "sphere displaced by seeded real spherical harmonics, l <= 4"},
+        "forward_steps": f1 - f0, "adjoint_steps": b1 - b0, "episodes": episodes, "clocks": clk.summary(),
+    }
+
+
 def run_e2e(torch, dm, args, w, device, keep):
     """Public API with pinned host buffers: x0, v0, F0 in; dL/dx_T seed in
     (computed on the host from x_T out, like run.py's gradient injection);
@@ -468,7 +542,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="spheres2m", choices=["spheres2m", "ellipsoid64", "sphere32", "batched"])
+    ap.add_argument("--workload", default="spheres2m",
+                    choices=["spheres2m", "ellipsoid64", "sphere32", "batched", "morph500k"])
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-particles", type=int, default=0, help="0: every particle")
     ap.add_argument("--cpu-timesteps", type=int, default=2)
@@ -501,6 +576,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=device)
     import build_oracle  # noqa: F401  (oracle build for the CPU baseline happens lazily)
+    if args.workload == "morph500k":
+        if rank == 0:
+            print(json.dumps(run_morph(args, device)), flush=True)
+        return
     line = run_ours(args, rank, world, device)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -103,6 +103,9 @@ typedef struct mpm_opt_input {
     int num_timesteps, control_stride, max_gd_iters, max_ls_iters, current_episodes;
     double dt, drag, smoothing_factor, initial_alpha, gd_tol;
     double f_ext[3];
+    /* additive: passes over the control steps (0: the reference's 3,
+       CompGraph.cpp:245) */
+    int passes;
 } mpm_opt_input;
 
 typedef struct mpm_pointcloud mpm_pointcloud;
@@ -210,6 +213,14 @@ int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int timestep_idx, 
                                            int current_episode, double initial_alpha, int max_line_search_iters);
 /* OptimizeDefGradControlSequence (CompGraph.cpp:213-368; bind.cpp:165-172) */
 int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt);
+/* No counterpart in the reference (which prints them): every loss the last
+ * run_optimization evaluated, in order -- the initial loss, per gradient
+ * step the loss before the step and each line-search trial, and the final
+ * loss.  *count receives the total; at most cap values are copied. */
+int mpm_compgraph_loss_history(const mpm_compgraph* cg, double* out, int cap, int* count);
+/* forward and adjoint particle steps executed since load (recomputed
+ * forward steps of checkpointed backward passes count as forward steps) */
+void mpm_step_count(long long* forward_steps, long long* backward_steps);
 /* number of grid nodes with mass > 0 in the forward grid of `layer` */
 int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long* out);
 /* number of grid nodes with mass > 0 in the forward grid of `layer` (the

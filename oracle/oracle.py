@@ -259,6 +259,88 @@ class Oracle:
         return xT, g
 
 
+    # -- CompGraph optimiser
+    def run_optimization(self, grid: Grid, prm: Params, s0: State, target_m, num_steps: int, control_stride: int,
+                         max_gd_iters: int, max_ls_iters: int, initial_alpha: float, gd_tol: float,
+                         passes: int = 3):
+        """OptimizeDefGradControlSequence (CompGraph.cpp:213-368) over the
+        FP64 step, loss and Adam of this oracle.  Returns every loss it
+        evaluates, in order (initial; per gradient step the loss before the
+        step and each line-search trial; final), and the final layers.
+
+        As in the reference: a forward pass from layer t rewrites layers
+        t+1.. and zeroes their control (ForwardSimulation.cpp:155), so a
+        rejected line-search trial leaves its states in the later layers;
+        Adam moments live per layer and are restored with dFc on rejection
+        (CompGraph.cpp:309-346); the control gradient is dL/dF of the
+        control layer, or dL/d(F + dFc) for the exact adjoint."""
+        L = int(num_steps)
+        n = s0.n
+        first = State(s0.x, s0.v, s0.C, s0.F, s0.m, s0.vol, s0.lam, s0.mu,
+                      s0.dFc if s0.dFc is not None else np.zeros((n, 3, 3)))
+        layers = [first] + [None] * (L - 1)
+        steps = [None] * (L - 1)
+        moments = {}
+        hist = []
+
+        def forward(start):  # ComputeForwardPass (CompGraph.cpp:131-141)
+            for i in range(start, L - 1):
+                nxt, st = self.forward_step(grid, prm, layers[i])
+                nxt.dFc = np.zeros((n, 3, 3))
+                layers[i + 1], steps[i] = nxt, st
+
+        def eval_loss():  # EndLayerMassLoss (CompGraph.cpp:42-129)
+            loss, aux = self.mass_loss(grid, prm, layers[-1].x, layers[-1].m, target_m)
+            hist.append(loss)
+            return loss, aux["gx"]
+
+        def backward(ctl, gx):  # ComputeBackwardPass (CompGraph.cpp:143-211)
+            g = Grads(np.array(gx, np.float64), np.zeros((n, 3)), np.zeros((n, 3, 3)), np.zeros((n, 3, 3)))
+            for t in range(L - 2, ctl - 1, -1):
+                g = self.backward_step(grid, prm, layers[t], layers[t + 1].C, steps[t], g, want_ft=(t == ctl))
+            return g.Ft if prm.exact else g.F
+
+        forward(0)
+        _, gx = eval_loss()
+        backward(0, gx)
+        adam_t = 0
+        for _ in range(passes):
+            for ct in range(0, L - 1, max(1, control_stride)):
+                alpha, init_norm = initial_alpha, 0.0
+                for it in range(max_gd_iters):
+                    forward(ct)
+                    loss, gx = eval_loss()
+                    if not np.isfinite(loss):
+                        break
+                    gc = backward(ct, gx)
+                    gn = max(self.grad_norm(gc), 1e-12)
+                    if it == 0:
+                        init_norm = gn
+                    if gn < gd_tol * init_norm:
+                        break
+                    lay = layers[ct]
+                    mom = moments.setdefault(ct, [np.zeros((n, 3, 3)) for _ in range(3)])
+                    bak = [lay.dFc.copy()] + [a.copy() for a in mom]
+                    ok, a = False, alpha
+                    for _ls in range(max_ls_iters):
+                        self.adam(gc, lay.dFc, mom[0], mom[1], mom[2], a, gn, timestep=adam_t + 1)
+                        forward(ct)
+                        nl, _ = eval_loss()
+                        if np.isfinite(nl) and nl < loss:
+                            adam_t += 1
+                            alpha = min(a * 1.1, initial_alpha)
+                            ok = True
+                            break
+                        lay.dFc[...] = bak[0]
+                        for dst, src in zip(mom, bak[1:]):
+                            dst[...] = src
+                        a *= 0.5
+                    if not ok:
+                        break
+        eval_loss()
+        return np.array(hist), layers
+
+
 class Reference:
     """The reference's own DiffMPMLib3D compiled from source (float or double)."""
 
@@ -356,3 +438,23 @@ class Reference:
                              _p(s.vol), _p(s.lam), _p(s.mu), _p(_f64(seed_gx)), _p(xT),
                              _p(g.x), _p(g.v), _p(g.F), _p(g.C), C.byref(tf), C.byref(tb))
         return xT, g, (tf.value, tb.value)
+
+    def optimize(self, grid: Grid, prm: Params, s: State, target_m, num_steps: int, control_stride: int,
+                 max_gd_iters: int, max_ls_iters: int, initial_alpha: float, gd_tol: float):
+        """The reference's OptimizeDefGradControlSequence (3 passes, reference
+        adjoint): final loss, every layer's dFc (L,N,3,3), last positions and
+        the optimiser's printed lines."""
+        dims, dx, mn = self._g(grid)
+        n = s.n
+        dfc = np.zeros((num_steps, n, 3, 3))
+        xT = np.zeros((n, 3))
+        log = C.create_string_buffer(1 << 16)
+        fext = np.asarray(prm.f_ext, dtype=np.float64)
+        self.lib.ref_optimize.restype = C.c_double
+        loss = self.lib.ref_optimize(dims, dx, _p(mn), C.c_double(prm.dt), C.c_double(prm.drag),
+                                     C.c_double(prm.smoothing), _p(fext), C.c_int(n), _p(s.x), _p(s.v), _p(s.F),
+                                     _p(s.m), _p(s.vol), _p(s.lam), _p(s.mu), _p(_f64(target_m)),
+                                     C.c_int(num_steps), C.c_int(control_stride), C.c_int(max_gd_iters),
+                                     C.c_int(max_ls_iters), C.c_double(initial_alpha), C.c_double(gd_tol),
+                                     _p(dfc), _p(xT), log, C.c_int(len(log)))
+        return loss, dfc, xT, log.value.decode(errors="replace")

@@ -19,7 +19,10 @@
 #include "Elasticity.h"
 
 #include <cstdio>
+#include <cstring>
 #include <memory>
+#include <sstream>
+#include <string>
 
 using namespace DiffMPMLib3D;
 typedef Vec3::Scalar Real;
@@ -274,6 +277,40 @@ int ref_rollout(const int* dims, double dx, const double* mn, double dt, double 
         put(q.dLdC, gC0 + 9 * p);
     }
     return 0;
+}
+
+// OptimizeDefGradControlSequence (CompGraph.cpp:213-368) as shipped (3
+// passes, reference adjoint) on a graph built from arrays.  Returns the
+// final loss and writes the control dFc of every layer (L = num_steps
+// layers, (L,N,3,3)) and the last layer's positions.  The optimiser's own
+// progress lines (initial/final loss) go to `log` (cap bytes) when given.
+double ref_optimize(const int* dims, double dx, const double* mn, double dt, double drag, double smoothing,
+                    const double* fext, int n, const double* x0, const double* v0, const double* F0,
+                    const double* m, const double* vol, const double* lam, const double* mu, const double* target_m,
+                    int num_steps, int control_stride, int max_gd, int max_ls, double alpha, double gd_tol,
+                    double* dFc_out, double* xT, char* log, int cap)
+{
+    auto pc = make_pc(n, x0, v0, nullptr, F0, nullptr, m, vol, lam, mu);
+    auto grid = make_grid(dims, dx, mn);
+    auto tgt = make_grid(dims, dx, mn);
+    for (size_t i = 0; i < tgt->nodes.size(); ++i) tgt->nodes[i].m = (Real)target_m[i];
+    std::ostringstream text;
+    std::streambuf* old = std::cout.rdbuf(text.rdbuf());
+    CompGraph cg(pc, grid, tgt);
+    cg.OptimizeDefGradControlSequence(num_steps, (Real)dt, (Real)drag, vec(fext), control_stride, max_gd, max_ls,
+                                      (Real)alpha, (Real)gd_tol, (Real)smoothing, 0);
+    double loss = cg.EndLayerMassLoss();
+    std::cout.rdbuf(old);
+    if (log && cap > 0) {
+        const std::string t = text.str();
+        const size_t k = std::min(t.size(), (size_t)cap - 1);
+        memcpy(log, t.data(), k);
+        log[k] = 0;
+    }
+    for (size_t l = 0; l < cg.layers.size(); ++l)
+        for (int p = 0; p < n; ++p) put(cg.layers[l].point_cloud->points[p].dFc, dFc_out + (l * n + p) * 9);
+    for (int p = 0; p < n; ++p) put(cg.layers.back().point_cloud->points[p].x, xT + 3 * p);
+    return loss;
 }
 
 }  // extern "C"

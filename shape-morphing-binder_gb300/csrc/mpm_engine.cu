@@ -532,7 +532,7 @@ struct Graph {
         std::vector<unsigned long long> sig;
         int seen = 0;
         cudaGraphExec_t exec = nullptr;
-        long long launches = 0;
+        long long launches = 0, fsteps = 0, bsteps = 0;
         std::vector<Prof::Rec> events;
         bool prof = false;
         ~Cap()
@@ -554,6 +554,7 @@ struct Graph {
     std::vector<InstHost> inst;
     Buf inst_table;
     long long total_nodes = 0;
+    std::vector<double> loss_hist;  // losses evaluated by the last run_optimization
     // render gradients (stored on the host like CompGraph.h:73-76)
     std::vector<float> rgF, rgx;
     bool has_rg = false;
@@ -677,10 +678,13 @@ void check_fix(Graph& G)
     }
 }
 
+long long g_fwd_steps = 0, g_bwd_steps = 0;  // particle-layer steps executed (host count)
+
 // One forward step: layer i -> layer i+1 (ForwardSimulation.cpp:159-185)
 template <typename R>
 void step_forward(const StepCfg& c, PCData& a, PCData& b, Buf& grid, Buf& trust, cudaStream_t s)
 {
+    ++g_fwd_steps;
     const long long nn = c.nodes();
     ensure(grid, sizeof(R) * 4 * nn, s, false);
     // the deterministic grid update writes every node
@@ -712,6 +716,7 @@ template <typename R>
 void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& grid, const Buf& trust,
                    cudaStream_t s)
 {
+    ++g_bwd_steps;
     const long long nn = c.nodes();
     if (!grid) fail(MPM_ERR_STATE, "backward pass before the forward pass of this step");
     ensure(G.adj, sizeof(R) * 4 * nn, s, false);
@@ -819,6 +824,8 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
     };
     if (c.exec && c.sig == sig.v) {
         g_launches += c.launches;
+        g_fwd_steps += c.fsteps;
+        g_bwd_steps += c.bsteps;
         replay();
         return;
     }
@@ -839,7 +846,7 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
         body();  // eager: allocations and attribute setup happen here
         return;
     }
-    const long long l0 = g_launches;
+    const long long l0 = g_launches, f0 = g_fwd_steps, b0 = g_bwd_steps;
     const size_t e0 = g_prof.pending.size();
     ck(cudaStreamBeginCapture(G.stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     g_prof.capturing = true;
@@ -860,6 +867,8 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
     cudaGraphDestroy(graph);
     ck(e, "cudaGraphInstantiate");
     c.launches = g_launches - l0;
+    c.fsteps = g_fwd_steps - f0;
+    c.bsteps = g_bwd_steps - b0;
     c.events.assign(g_prof.pending.begin() + e0, g_prof.pending.end());
     g_prof.pending.resize(e0);
     c.prof = g_prof.on;
@@ -1198,7 +1207,13 @@ void graph_run_optimization(Graph& G, const mpm_opt_input& o)
     say("Optimizing with num_steps=%d, dt=%g, drag=%g\n", o.num_timesteps, o.dt, o.drag);
     graph_set_up<R>(G, o.num_timesteps);
     graph_forward<R>(G, 0);
-    double init_loss = graph_loss<R>(G);
+    G.loss_hist.clear();
+    auto eval_loss = [&]() {
+        const double l = graph_loss<R>(G);
+        G.loss_hist.push_back(l);
+        return l;
+    };
+    double init_loss = eval_loss();
     say("Initial loss = %g\n", init_loss);
     graph_backward<R>(G, 0);
     say("Initial global gradient norm = %g\n", graph_grad_norm<R>(G, 0));
@@ -1206,7 +1221,7 @@ void graph_run_optimization(Graph& G, const mpm_opt_input& o)
     int adam_t = 0;
     cudaStream_t s = G.stream;
     Backup bk;
-    const int passes = 3;
+    const int passes = o.passes > 0 ? o.passes : 3;
     say("Number of Iteration Passes: %d\n", passes);
     for (int pass = 0; pass < passes; ++pass) {
         for (int ct = 0; ct < o.num_timesteps - 1; ct += std::max(1, o.control_stride)) {
@@ -1214,7 +1229,7 @@ void graph_run_optimization(Graph& G, const mpm_opt_input& o)
             double alpha = o.initial_alpha, init_norm = 0;
             for (int it = 0; it < o.max_gd_iters; ++it) {
                 graph_forward<R>(G, ct);
-                double loss = graph_loss<R>(G);
+                double loss = eval_loss();
                 if (!std::isfinite(loss)) {
                     say("Warning: Non-finite loss detected. Aborting step.\n");
                     break;
@@ -1233,7 +1248,7 @@ void graph_run_optimization(Graph& G, const mpm_opt_input& o)
                 for (int ls = 0; ls < o.max_ls_iters; ++ls) {
                     graph_adam<R>(G, ct, a, gn, beta1, beta2, eps, adam_t + 1);
                     graph_forward<R>(G, ct);
-                    double nl = graph_loss<R>(G);
+                    double nl = eval_loss();
                     if (std::isfinite(nl) && nl < loss) {
                         ++adam_t;
                         alpha = std::min(a * 1.1, o.initial_alpha);
@@ -1250,7 +1265,7 @@ void graph_run_optimization(Graph& G, const mpm_opt_input& o)
             }
         }
     }
-    say("Final loss = %g\n", graph_loss<R>(G));
+    say("Final loss = %g\n", eval_loss());
     say("Optimization finished.\n");
 }
 
@@ -1868,6 +1883,23 @@ int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt)
         ck(cudaStreamSynchronize(cg->g.stream), "run_optimization");
         check_fix(cg->g);
     });
+}
+
+int mpm_compgraph_loss_history(const mpm_compgraph* cg, double* out, int cap, int* count)
+{
+    return guard([&] {
+        check_cg(cg);
+        const auto& h = cg->g.loss_hist;
+        if (count) *count = (int)h.size();
+        if (out)
+            for (int i = 0; i < cap && i < (int)h.size(); ++i) out[i] = h[i];
+    });
+}
+
+void mpm_step_count(long long* forward_steps, long long* backward_steps)
+{
+    if (forward_steps) *forward_steps = g_fwd_steps;
+    if (backward_steps) *backward_steps = g_bwd_steps;
 }
 
 int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long* out)

@@ -431,14 +431,26 @@ class CompGraph:
         check(lib.mpm_compgraph_synchronize(self._h))
 
     # -- reference surface
-    def run_optimization(self, opt: OptInput):
+    def run_optimization(self, opt: OptInput, *, passes: int | None = None):
+        """OptimizeDefGradControlSequence (CompGraph.cpp:213-368).  ``passes``
+        (additive) replaces the reference's fixed 3 passes over the control
+        steps."""
         o = MpmOptInput()
+        o.passes = int(passes or 0)
         o.num_timesteps, o.control_stride = opt.num_timesteps, opt.control_stride
         o.max_gd_iters, o.max_ls_iters, o.current_episodes = opt.max_gd_iters, opt.max_ls_iters, opt.current_episodes
         o.dt, o.drag, o.smoothing_factor = opt.dt, opt.drag, opt.smoothing_factor
         o.initial_alpha, o.gd_tol = opt.initial_alpha, opt.gd_tol
         o.f_ext[:] = [float(v) for v in opt.f_ext]
         check(lib.mpm_compgraph_run_optimization(self._h, C.byref(o)), "run_optimization")
+
+    def loss_history(self) -> np.ndarray:
+        """Every loss the last run_optimization evaluated, in order (additive)."""
+        n = C.c_int()
+        check(lib.mpm_compgraph_loss_history(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        check(lib.mpm_compgraph_loss_history(self._h, out.ctypes.data_as(_lib._dp), n.value, C.byref(n)))
+        return out
 
     def get_num_layers(self) -> int:
         n = C.c_int()
@@ -595,3 +607,10 @@ def load_point_cloud_from_obj(obj_path: str, opt: OptInput, precision=None) -> P
     return PointCloud.from_arrays(pts.astype(np.float32), m=np.full(n, m, np.float32),
                                   vol=np.full(n, vol, np.float32), lam=np.full(n, opt.lam, np.float32),
                                   mu=np.full(n, opt.mu, np.float32), precision=precision)
+
+
+def step_count():
+    """(forward, adjoint) particle-layer steps executed since load (additive)."""
+    f, b = C.c_longlong(), C.c_longlong()
+    lib.mpm_step_count(C.byref(f), C.byref(b))
+    return f.value, b.value

@@ -40,7 +40,7 @@ class MpmOptInput(C.Structure):
     _fields_ = [("num_timesteps", C.c_int), ("control_stride", C.c_int), ("max_gd_iters", C.c_int),
                 ("max_ls_iters", C.c_int), ("current_episodes", C.c_int), ("dt", C.c_double),
                 ("drag", C.c_double), ("smoothing_factor", C.c_double), ("initial_alpha", C.c_double),
-                ("gd_tol", C.c_double), ("f_ext", C.c_double * 3)]
+                ("gd_tol", C.c_double), ("f_ext", C.c_double * 3), ("passes", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -99,6 +99,8 @@ _SIGS = {
     "mpm_compgraph_use_graphs": [_vp, C.c_int],
     "mpm_compgraph_set_tuning": [_vp, C.c_int, C.c_int],
     "mpm_compgraph_set_deterministic": [_vp, C.c_int],
+    "mpm_compgraph_loss_history": [_vp, _dp, C.c_int, _ip],
+    "mpm_step_count": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "mpm_compgraph_get_tuning": [_vp, _ip, _ip],
     "mpm_compgraph_autotune": [_vp, C.c_int, _ip, _ip, _dp],
     "mpm_compgraph_synchronize": [_vp],
@@ -110,7 +112,7 @@ _SIGS = {
     "mpm_mass_loss_noalloc": [C.c_int, _vp, _vp, _vp, _ip, C.c_double, _dp, C.c_int, _vp, _dp, _vp],
 }
 _RESTYPE = {"mpm_last_error": C.c_char_p, "mpm_kernel_name": C.c_char_p, "mpm_launch_count": C.c_longlong, "mpm_default_params": None, "mpm_default_options": None,
-            "mpm_set_verbose": None}
+            "mpm_set_verbose": None, "mpm_step_count": None}
 
 
 class MpmError(RuntimeError):

@@ -36,6 +36,11 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_opt():
+    return dict(np.load(ROOT / "tests" / "golden" / "reference_optimize.npz"))
+
+
+@pytest.fixture(scope="session")
 def dm():
     import diffmpm_bindings
     diffmpm_bindings._lib.lib.mpm_set_verbose(0)

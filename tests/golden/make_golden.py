@@ -5,10 +5,12 @@ Runs where the reference tree is mounted: it builds oracle/_ref/libref{32,64}.so
 the reference's ForwardTimeStep, Back_Timestep, EndLayerMassLoss,
 Descend_Adam, CalculatePointCloudVolumes, PK_FixedCorotatedElasticity and
 d2_FCE_psi_dF2_mult_by_dF, plus a 5-step full-tape forward/backward through
-CompGraph.  The fixtures (tests/golden/*.npz) travel with the repository;
-the GPU tests compare against them without the reference present.
+CompGraph (reference_small.npz), and a run of the control-sequence
+optimiser OptimizeDefGradControlSequence (reference_optimize.npz).  The
+fixtures travel with the repository; the GPU tests compare against them
+without the reference present.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [--only small|optimize]
 """
 from __future__ import annotations
 
@@ -39,11 +41,47 @@ def small_state(seed=7, G=10, rng_scale=1.0):
     return w, s, rng
 
 
-def main():
+OPT_CASE = dict(num_steps=6, control_stride=2, max_gd_iters=2, max_ls_iters=4, initial_alpha=0.05, gd_tol=1e-4)
+
+
+def optimize_case():
+    """Inputs of the optimiser fixture: 524 particles at rest-state F = I,
+    C = 0; target masses from the particles shifted by (0.04, 0, 0.02)."""
+    w = W.sphere32(seed=7, G=10)
+    n = w.n
+    s = O.State(w.x, w.v, np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), w.m, w.vol, w.lam, w.mu)
+    g = O.Grid(w.dims, w.dx)
+    tgt = np.zeros(g.n_nodes)
+    O.Oracle().p2g_accumulate(g, w.x + np.array([0.04, 0.0, 0.02]), w.v, np.zeros((n, 3, 3)), w.m, tgt,
+                              np.zeros((g.n_nodes, 3)))
+    prm = O.Params(dt=1e-3, drag=0.5, smoothing=0.1)
+    return w, s, g, tgt, prm
+
+
+def make_optimize():
+    r64, r32 = O.Reference(64), O.Reference(32)
+    w, s, g, tgt, prm = optimize_case()
+    rec = dict(dims=np.asarray(w.dims), dx=w.dx, dt=prm.dt, drag=prm.drag, smoothing=prm.smoothing, target=tgt,
+               x=s.x, v=s.v, m=s.m, vol=s.vol, lam=s.lam, mu=s.mu, **{k: v for k, v in OPT_CASE.items()})
+    for bits, ref in ((64, r64), (32, r32)):
+        loss, dfc, xT, log = ref.optimize(g, prm, s, tgt, **OPT_CASE)
+        rec[f"opt{bits}_loss"] = loss
+        rec[f"opt{bits}_dFc"] = dfc
+        rec[f"opt{bits}_xT"] = xT
+        rec[f"opt{bits}_initial_loss"] = float(log.split("Initial loss = ")[1].split()[0])
+    np.savez_compressed(OUT / "reference_optimize.npz", **rec)
+    print("wrote", OUT / "reference_optimize.npz", "N =", s.n)
+
+
+def main(which=("small", "optimize")):
     build_oracle.build_oracle()
     outs = build_oracle.build_ref()
     if not outs:
         raise SystemExit("reference tree not found; golden vectors need the reference sources")
+    if "optimize" in which:
+        make_optimize()
+    if "small" not in which:
+        return
     r64, r32 = O.Reference(64), O.Reference(32)
     w, s, rng = small_state()
     g = O.Grid(w.dims, w.dx)
@@ -117,4 +155,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["small", "optimize"])
+    a = ap.parse_args()
+    main((a.only,) if a.only else ("small", "optimize"))

@@ -95,3 +95,16 @@ def oracle_loss(orc, grid, prm, s0, T, seed_gx):
     for _ in range(T):
         s, _ = orc.forward_step(grid, prm, s)
     return float((np.asarray(seed_gx).reshape(-1, 3) * s.x).sum())
+
+
+def golden_opt_case(go):
+    """State, grid, target and optimiser arguments of reference_optimize.npz."""
+    import oracle as O
+    n = len(go["m"])
+    s = O.State(go["x"], go["v"], np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), go["m"], go["vol"],
+                go["lam"], go["mu"])
+    g = O.Grid(tuple(int(d) for d in go["dims"]), float(go["dx"]))
+    prm = O.Params(dt=float(go["dt"]), drag=float(go["drag"]), smoothing=float(go["smoothing"]))
+    kw = {k: (float(go[k]) if k in ("initial_alpha", "gd_tol") else int(go[k]))
+          for k in ("num_steps", "control_stride", "max_gd_iters", "max_ls_iters", "initial_alpha", "gd_tol")}
+    return s, g, go["target"], prm, kw

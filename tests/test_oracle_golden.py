@@ -82,3 +82,20 @@ def test_float_reference_noise_floor(golden):
     assert rel_err(golden["fwd32_x"], golden["fwd64_x"]) < 1e-6
     assert rel_err(golden["fwd32_C"], golden["fwd64_C"]) < 2e-3
     assert rel_err(golden["roll32_xT"], golden["roll64_xT"]) < 1e-6
+
+
+def test_optimizer_matches_reference(orc, golden_opt):
+    """OptimizeDefGradControlSequence (CompGraph.cpp:213-368): the oracle's
+    restatement reproduces the reference's recorded run (3 passes, line
+    search with rejections) -- every layer's control, the final positions and
+    the initial/final loss."""
+    from helpers import golden_opt_case
+    s, g, tgt, prm, kw = golden_opt_case(golden_opt)
+    hist, layers = orc.run_optimization(g, prm, s, tgt, **kw)
+    assert abs(hist[0] - golden_opt["opt64_initial_loss"]) <= 1e-5 * hist[0]  # printed with 6 digits
+    assert abs(hist[-1] - golden_opt["opt64_loss"]) <= 1e-12 * hist[-1]
+    assert hist[-1] < hist[0]
+    want = golden_opt["opt64_dFc"]
+    for l, lay in enumerate(layers):
+        assert rel_err(lay.dFc, want[l]) < 1e-10 if np.abs(want[l]).max() > 0 else np.abs(lay.dFc).max() == 0
+    assert rel_err(layers[-1].x, golden_opt["opt64_xT"]) < 1e-13

@@ -43,3 +43,25 @@ def test_inverted_and_degenerate_stress(orc, ref64):
         dF = rng.normal(size=(3, 3))
         assert rel_err(orc.pk(F, 100.0, 50.0), ref64.pk(F, 100.0, 50.0)) < 1e-8
         assert rel_err(orc.pk_vjp(F, 100.0, 50.0, dF), ref64.hvp(F, 100.0, 50.0, dF)) < 1e-7
+
+
+def test_optimizer_random_case(orc, ref64):
+    """The oracle's OptimizeDefGradControlSequence against the reference's on
+    another seeded case (drag, smoothing and gravity on)."""
+    from diffmpm_bindings import workloads as W
+    w = W.sphere32(seed=11, G=9)
+    n = w.n
+    rng = np.random.default_rng(11)
+    s = O.State(w.x, w.v, np.zeros((n, 3, 3)), np.eye(3) + 0.02 * rng.normal(size=(n, 3, 3)), w.m, w.vol, w.lam,
+                w.mu)
+    g = O.Grid(w.dims, w.dx)
+    tgt = np.zeros(g.n_nodes)
+    orc.p2g_accumulate(g, w.x * 0.95 + 0.03, w.v, np.zeros((n, 3, 3)), w.m, tgt, np.zeros((g.n_nodes, 3)))
+    prm = O.Params(dt=1e-3, drag=0.3, smoothing=0.2, f_ext=(0.0, -2.0, 0.0))
+    kw = dict(num_steps=7, control_stride=3, max_gd_iters=3, max_ls_iters=3, initial_alpha=0.1, gd_tol=1e-4)
+    hist, layers = orc.run_optimization(g, prm, s, tgt, **kw)
+    loss, dfc, xT, _ = ref64.optimize(g, prm, s, tgt, **kw)
+    assert abs(hist[-1] - loss) <= 1e-11 * loss
+    for l, lay in enumerate(layers):
+        assert np.abs(lay.dFc - dfc[l]).max() <= 1e-10 * max(1.0, np.abs(dfc[l]).max())
+    assert rel_err(layers[-1].x, xT) < 1e-12
