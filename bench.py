@@ -334,7 +334,10 @@ def run_morph(args, device):
                                     lam=w0.lam.astype(np.float32), mu=w0.mu.astype(np.float32))
     grid = dm.Grid(*w0.dims, w0.dx, w0.grid_min)
     target = dm.Grid(*w0.dims, w0.dx, w0.grid_min)
-    cg = dm.CompGraph(pc0, grid, target, checkpoint_every=10, deterministic=True)
+    # exact adjoint: the reference-compatible one repeats (I + dt C)^T dL/dF
+    # (BackPropagation.cpp:140), which doubles dL/dF every step -- 2^200 over a
+    # 200-step pass, beyond the FP32 range
+    cg = dm.CompGraph(pc0, grid, target, checkpoint_every=10, deterministic=not args.no_det, adjoint="exact")
     opt = dm.OptInput()
     opt.num_timesteps, opt.control_stride, opt.max_gd_iters, opt.max_ls_iters = steps + 1, 10, 1, 4
     opt.dt, opt.drag, opt.smoothing_factor = w0.dt, w0.drag, w0.smoothing
@@ -363,7 +366,8 @@ def run_morph(args, device):
             total += dt_e
             h = cg.loss_history()
             episodes.append({"episode": e, "seconds": round(dt_e, 3), "initial_loss": float(h[0]),
-                             "final_loss": float(h[-1]), "losses_evaluated": int(len(h))})
+                             "final_loss": float(h[-1]), "best_loss": float(np.nanmin(h)),
+                             "losses_evaluated": int(len(h)), "nonfinite_trials": int((~np.isfinite(h)).sum())})
             cg.promote_last_as_initial()
     f1, b1 = dm.step_count()
     psteps = n * ((f1 - f0) + (b1 - b0))
@@ -376,7 +380,7 @@ def run_morph(args, device):
         "config": {"workload": "morph500k" if not args.quick else "morph50k", "particles": n,
                    "grid_nodes": list(w0.dims), "dx": w0.dx, "timesteps_per_pass": steps, "control_stride": 10,
                    "passes": passes, "episodes": args.steps, "lr": 1e-2, "max_line_search": 4,
-                   "checkpoint_every": 10, "deterministic": True, "adjoint": "reference",
+                   "checkpoint_every": 10, "deterministic": not args.no_det, "adjoint": "exact",
                    "target": "sphere displaced by seeded real spherical harmonics, l <= 4"},
         "forward_steps": f1 - f0, "adjoint_steps": b1 - b0, "episodes": episodes, "clocks": clk.summary(),
     }
@@ -555,6 +559,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--deterministic", action="store_true",
                     help="fixed-point node sums (bitwise reproducible passes)")
+    ap.add_argument("--no-det", action="store_true", help="morph500k: float atomics instead of fixed point")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -659,12 +659,16 @@ void begin_fix_pass(const Graph& G, const StepCfg& c, const PCData& d, cudaStrea
 {
     if (!c.det()) return;
     ck(cudaMemsetAsync(G.fix->p, 0, G.fix->bytes, s), "memset");
+    ck(cudaMemsetAsync(G.fctl->p, 0, G.fctl->bytes, s), "memset");  // overflow flags are per pass
     launch_fix_prepare(c, d.n, d.ld, d.co->as<float>(), s);
 }
 
 // overflow flags of the fixed-point accumulators, read and cleared after a
-// synchronised API call
-void check_fix(Graph& G)
+// synchronised API call.  An overflow makes that pass's results NaN (the
+// grid kernels poison the step); single passes report it, the optimisers
+// treat it like any non-finite trial (rejected, CompGraph.cpp:289-292,324)
+// and do not raise.
+void check_fix(Graph& G, bool raise = true)
 {
     if (!G.opt.deterministic || !G.fctl) return;
     unsigned f = 0;
@@ -673,6 +677,7 @@ void check_fix(Graph& G)
     if (f) {
         ck(cudaMemsetAsync(G.fctl->as<unsigned>() + 3, 0, sizeof f, G.stream), "memset");
         ck(cudaStreamSynchronize(G.stream), "sync");
+        if (!raise) return;
         fail(MPM_ERR_NONFINITE,
              "deterministic scatter: a node sum left the fixed-point range (non-finite or exploding state)");
     }
@@ -1869,7 +1874,7 @@ int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int t, int max_gd,
         check_cg(cg);
         with_prec(cg->g.prec, [&](auto r) { graph_optimize_single<decltype(r)>(cg->g, t, max_gd, episode, alpha, max_ls); });
         ck(cudaStreamSynchronize(cg->g.stream), "optimize");
-        check_fix(cg->g);
+        check_fix(cg->g, false);
     });
 }
 
@@ -1881,7 +1886,7 @@ int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt)
         if (opt->num_timesteps < 1) fail(MPM_ERR_ARG, "num_timesteps must be positive");
         with_prec(cg->g.prec, [&](auto r) { graph_run_optimization<decltype(r)>(cg->g, *opt); });
         ck(cudaStreamSynchronize(cg->g.stream), "run_optimization");
-        check_fix(cg->g);
+        check_fix(cg->g, false);
     });
 }
 

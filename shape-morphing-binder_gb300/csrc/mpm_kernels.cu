@@ -1013,8 +1013,14 @@ __global__ void k_grid_update_fix(KP<float> kp, long long nn, FixArgs fx, float*
     }
     const long long lim = 1ll << 62;
     if (q01.x >= lim || q01.x <= -lim || q01.y >= lim || q01.y <= -lim || q23.x >= lim || q23.x <= -lim ||
-        q23.y >= lim || q23.y <= -lim)
+        q23.y >= lim || q23.y <= -lim || (fx.ctl[3] & 1u)) {
+        // out of the fixed-point range (or a non-finite contribution this
+        // pass): the step's result is non-finite, as an overflowing float sum
+        // would make it
         atomicOr(&fx.ctl[3], 2u);
+        reinterpret_cast<float4*>(grid)[i] = make_float4(NAN, NAN, NAN, NAN);
+        return;
+    }
     float m = __ll2float_rn(q23.y) * im;
     if (m < 0.f) m = 0.f;
     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
@@ -1148,8 +1154,12 @@ __global__ void k_grid_adj_fix(KP<float> kp, long long nn, const float* __restri
         a[1] = make_longlong2(0, 0);
     }
     const long long lim = 1ll << 62;
-    if (q01.x >= lim || q01.x <= -lim || q01.y >= lim || q01.y <= -lim || q23.x >= lim || q23.x <= -lim)
+    if (q01.x >= lim || q01.x <= -lim || q01.y >= lim || q01.y <= -lim || q23.x >= lim || q23.x <= -lim ||
+        (fx.ctl[3] & 1u)) {
         atomicOr(&fx.ctl[3], 2u);
+        reinterpret_cast<float4*>(adj)[i] = make_float4(NAN, NAN, NAN, NAN);
+        return;
+    }
     const float d0 = __ll2float_rn(q01.x) * inv, d1 = __ll2float_rn(q01.y) * inv, d2 = __ll2float_rn(q23.x) * inv;
     const float4 g = reinterpret_cast<const float4*>(grid)[i];
     float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1475,7 +1485,7 @@ __global__ void k_fix_mass_out(long long nn, FixArgs fx, float* __restrict__ gm)
     if (i >= nn) return;
     const long long q = (long long)fx.acc[4 * i + 3];
     if (q) fx.acc[4 * i + 3] = 0ull;
-    gm[i] = __ll2float_rn(q) * pow2f(-fix_exponent(fix_mass_bound(fx)));
+    gm[i] = (fx.ctl[3] & 1u) ? NAN : __ll2float_rn(q) * pow2f(-fix_exponent(fix_mass_bound(fx)));
 }
 
 // Deterministic reductions: each block writes its partial sum(s) to
