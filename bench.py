@@ -209,9 +209,14 @@ def run_ours(args, rank, world, device):
         args.no_e2e, args.no_fp64, args.no_cpu = True, True, True
     else:
         w = make_workload(args.workload, args.quick, args.timesteps)
+        if args.shuffle:
+            p = np.random.default_rng(5).permutation(w.n)
+            for k in ("x", "v", "F", "m", "vol", "lam", "mu", "target"):
+                setattr(w, k, getattr(w, k)[p])
         n, T = w.n, w.steps
         cg, keep = build_graph(dm, w, "fp32", w.checkpoint, deterministic=args.deterministic)
         n_pad = n
+    cg.set_resort(not args.no_resort)
     cg.set_up_comp_graph(T + 1)
     stream = torch.cuda.current_stream(device)
     cg.set_stream(stream)
@@ -297,7 +302,9 @@ def run_ours(args, rank, world, device):
                    "kernel": "cubic B-spline APIC", "adjoint": "exact", "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed steps (256 MiB write, outside the event brackets)",
                    "bench_step": "one rollout: forward T steps + loss gradient + backward T steps",
-                   "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic)},
+                   "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic),
+                   "particle_order": ("shuffled" if args.shuffle else "cell-sorted input") +
+                                     ("" if args.no_resort else ", re-sorted by cell at set-up")},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
         "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
     }
@@ -560,6 +567,8 @@ def main():
     ap.add_argument("--deterministic", action="store_true",
                     help="fixed-point node sums (bitwise reproducible passes)")
     ap.add_argument("--no-det", action="store_true", help="morph500k: float atomics instead of fixed point")
+    ap.add_argument("--shuffle", action="store_true", help="shuffle the particle order of the workload")
+    ap.add_argument("--no-resort", action="store_true", help="keep the input particle order (no cell re-sort)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

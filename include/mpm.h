@@ -257,6 +257,15 @@ int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on);
  * the fixed-point range (a non-finite or exploding state) fails with
  * MPM_ERR_NONFINITE. */
 int mpm_compgraph_set_deterministic(mpm_compgraph* cg, int on);
+/* No counterpart in the reference (whose particles keep their order): order
+ * the graph's particles by (instance, grid cell) of layer 0's positions, the
+ * order the scatter and gather kernels run fastest in.  Every layer's planes
+ * move; the graph keeps the permutation and every get/set goes through it,
+ * so callers see their own particle order unchanged.  set_up_comp_graph (and
+ * so run_optimization) re-sorts by default; mpm_compgraph_set_resort(cg, 0)
+ * turns that off. */
+int mpm_compgraph_resort(mpm_compgraph* cg);
+int mpm_compgraph_set_resort(mpm_compgraph* cg, int on);
 /* accumulate dL/dlambda and dL/dmu per particle over the next backward
  * passes; read them from the control layer's MPM_FIELD_GRAD_LAM/GRAD_MU */
 int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on);

@@ -213,6 +213,11 @@ struct PCData {
     Buf gctl;             // 9 planes, control gradient (lazy; exact adjoint)
     Buf glame;            // 2 planes, dL/dlam and dL/dmu (lazy)
     Buf adam;             // 27 planes of double (lazy)
+    // slot p holds the caller's particle perm[p] (n ints; null: identity).
+    // A graph re-sorts its particles by cell and keeps the permutation here,
+    // shared by its layers; every copy in or out goes through it, so callers
+    // always see their own order.
+    Buf perm;
     bool have_state = true;
 
     size_t es() const { return esize(prec); }
@@ -269,6 +274,7 @@ std::shared_ptr<PCData> clone_pc(const PCData& a, cudaStream_t s, bool share_con
         d->adam = make_buf(a.adam->bytes, s, false);
         copy_buf(d->adam, a.adam, s);
     }
+    d->perm = a.perm;  // never changed in place: re-sorts install a new one
     return d;
 }
 
@@ -326,7 +332,8 @@ DevBuf& staging(size_t bytes)
 
 // Convert between a caller buffer (row-major, dtype, host/device) and planes.
 template <typename R>
-void planes_in(int n, int k, long long ld, const void* src, int dtype, int on_device, R* dst, cudaStream_t s)
+void planes_in(int n, int k, long long ld, const void* src, int dtype, int on_device, R* dst, cudaStream_t s,
+               const int* perm = nullptr)
 {
     if (n == 0) return;
     const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
@@ -337,14 +344,15 @@ void planes_in(int n, int k, long long ld, const void* src, int dtype, int on_de
         ck(cudaMemcpyAsync(tmp.p, src, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
         dsrc = tmp.p;
     }
-    if (dtype == MPM_DTYPE_F64) launch_aos_to_planes<R, double>(n, k, ld, (const double*)dsrc, dst, s);
-    else launch_aos_to_planes<R, float>(n, k, ld, (const float*)dsrc, dst, s);
+    if (dtype == MPM_DTYPE_F64) launch_aos_to_planes<R, double>(n, k, ld, (const double*)dsrc, dst, s, perm);
+    else launch_aos_to_planes<R, float>(n, k, ld, (const float*)dsrc, dst, s, perm);
     ck(cudaGetLastError(), "aos_to_planes");
     if (!on_device) ck(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
 
 template <typename R>
-void planes_out(int n, int k, long long ld, const R* src, void* dst, int dtype, int on_device, cudaStream_t s)
+void planes_out(int n, int k, long long ld, const R* src, void* dst, int dtype, int on_device, cudaStream_t s,
+                const int* perm = nullptr)
 {
     if (n == 0) return;
     const size_t tsz = dtype == MPM_DTYPE_F64 ? 8 : 4;
@@ -355,8 +363,8 @@ void planes_out(int n, int k, long long ld, const R* src, void* dst, int dtype, 
         tmp = &staging(bytes);
         ddst = tmp->p;
     }
-    if (dtype == MPM_DTYPE_F64) launch_planes_to_aos<R, double>(n, k, ld, src, (double*)ddst, s);
-    else launch_planes_to_aos<R, float>(n, k, ld, src, (float*)ddst, s);
+    if (dtype == MPM_DTYPE_F64) launch_planes_to_aos<R, double>(n, k, ld, src, (double*)ddst, s, perm);
+    else launch_planes_to_aos<R, float>(n, k, ld, src, (float*)ddst, s, perm);
     ck(cudaGetLastError(), "planes_to_aos");
     if (!on_device) {
         ck(cudaMemcpyAsync(dst, tmp->p, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
@@ -408,7 +416,7 @@ void pc_get(const PCData& d, int field, void* dst, int dtype, int on_device, cud
         base = tmp.as<R>();
         break;
     }
-    planes_out<R>(d.n, f.k, ld, base, dst, dtype, on_device, s);
+    planes_out<R>(d.n, f.k, ld, base, dst, dtype, on_device, s, d.perm ? d.perm->as<int>() : nullptr);
 }
 
 template <typename R>
@@ -429,7 +437,7 @@ void pc_set(PCData& d, int field, const void* src, int dtype, int on_device, cud
         break;
     default: fail(MPM_ERR_ARG, "field %d is read only", field);
     }
-    planes_in<R>(d.n, f.k, d.ld, src, dtype, on_device, base, s);
+    planes_in<R>(d.n, f.k, d.ld, src, dtype, on_device, base, s, d.perm ? d.perm->as<int>() : nullptr);
 }
 
 // ------------------------------------------------------------------- grids
@@ -555,6 +563,7 @@ struct Graph {
     Buf inst_table;
     long long total_nodes = 0;
     std::vector<double> loss_hist;  // losses evaluated by the last run_optimization
+    bool resort_on = true;           // re-sort the particles by cell at set-up
     // render gradients (stored on the host like CompGraph.h:73-76)
     std::vector<float> rgF, rgx;
     bool has_rg = false;
@@ -685,6 +694,71 @@ void check_fix(Graph& G, bool raise = true)
 
 long long g_fwd_steps = 0, g_bwd_steps = 0;  // particle-layer steps executed (host count)
 
+// Re-sort the graph's particles by (instance, cell) of layer 0's positions:
+// every particle plane of every layer (state, constants, control, gradients,
+// Adam moments, trust scales) moves to the new order in place, and the
+// layers get the composed permutation.  Grids do not depend on the order.
+template <typename R>
+void graph_resort(Graph& G)
+{
+    PCData& d0 = *G.layers[0].pc;
+    if (!d0.have_state || d0.n <= 1) return;
+    cudaStream_t s = G.stream;
+    const int n = d0.n;
+    const long long ld = d0.ld;
+    StepCfg c = G.cfg();
+    DevBuf order(sizeof(int) * n);
+    ck(cudaStreamSynchronize(s), "sync");
+    if (!cell_order<R>(c, G.inst.empty() ? nullptr : G.inst.data(), (int)G.inst.size(), n, ld,
+                       d0.st->as<R>() + ST_X * ld, order.as<int>(), s))
+        fail(MPM_ERR_CUDA, "particle re-sort: %s", cudaGetErrorString(cudaGetLastError()));
+    check_launch("cell_order");
+    size_t big = 0;
+    std::vector<std::pair<DevBuf*, int>> todo;  // buffer, element size
+    auto add = [&](const Buf& b, int es) {
+        if (!b) return;
+        for (auto& t : todo)
+            if (t.first == b.get()) return;  // shared (the constants)
+        todo.push_back({b.get(), es});
+        big = std::max(big, b->bytes);
+    };
+    for (Layer& L : G.layers) {
+        if (!L.pc) continue;
+        PCData& d = *L.pc;
+        if (d.have_state) add(d.st, (int)sizeof(R));
+        add(d.co, (int)sizeof(R));
+        if (!d.dfc_zero) add(d.dfc, (int)sizeof(R));
+        add(d.grads, (int)sizeof(R));
+        add(d.gctl, (int)sizeof(R));
+        add(d.glame, (int)sizeof(R));
+        add(d.adam, 8);
+        add(L.trust, (int)sizeof(R));
+    }
+    DevBuf tmp(big);
+    for (auto& t : todo) {
+        const int planes = (int)(t.first->bytes / ((size_t)t.second * ld));
+        if (planes <= 0) continue;
+        if (t.second == 8)
+            launch_gather_planes<double>(n, planes, ld, order.as<int>(), t.first->as<double>(), tmp.as<double>(), s);
+        else
+            launch_gather_planes<float>(n, planes, ld, order.as<int>(), t.first->as<float>(), tmp.as<float>(), s);
+        ck(cudaMemcpyAsync(t.first->p, tmp.p, (size_t)planes * ld * t.second, cudaMemcpyDeviceToDevice, s), "copy");
+    }
+    // perm_new[i] = perm_old[order[i]]
+    Buf perm = make_buf(sizeof(int) * n, s, false);
+    if (d0.perm) launch_gather_planes<float>(n, 1, n, order.as<int>(), d0.perm->as<float>(), perm->as<float>(), s);
+    else ck(cudaMemcpyAsync(perm->p, order.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s), "copy");
+    check_launch("resort");
+    ck(cudaStreamSynchronize(s), "sync");
+    for (Layer& L : G.layers)
+        if (L.pc) L.pc->perm = perm;
+    G.base->perm = perm;
+    for (auto* q : {&G.ping, &G.pong})
+        if (*q) (*q)->perm = perm;
+    for (auto& q : G.seg)
+        if (q) q->perm = perm;
+}
+
 // One forward step: layer i -> layer i+1 (ForwardSimulation.cpp:159-185)
 template <typename R>
 void step_forward(const StepCfg& c, PCData& a, PCData& b, Buf& grid, Buf& trust, cudaStream_t s)
@@ -766,6 +840,7 @@ std::shared_ptr<PCData> shell_like(const PCData& a, cudaStream_t s, bool with_st
     d->dfc = make_buf(a.planes_bytes(9), s, false);
     d->dfc_zero = true;
     d->have_state = with_state;
+    d->perm = a.perm;
     return d;
 }
 
@@ -946,8 +1021,9 @@ void inject_render_grads(Graph& G)
     cudaStream_t s = G.stream;
     ensure_grads(last, s);
     DevBuf tmp((size_t)12 * last.ld * sizeof(R));
-    planes_in<R>(last.n, 9, last.ld, G.rgF.data(), MPM_DTYPE_F32, 0, tmp.as<R>(), s);
-    planes_in<R>(last.n, 3, last.ld, G.rgx.data(), MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s);
+    const int* perm = last.perm ? last.perm->as<int>() : nullptr;
+    planes_in<R>(last.n, 9, last.ld, G.rgF.data(), MPM_DTYPE_F32, 0, tmp.as<R>(), s, perm);
+    planes_in<R>(last.n, 3, last.ld, G.rgx.data(), MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s, perm);
     launch_axpy_planes<R>(last.n, 9, last.ld, R(1), tmp.as<R>(), last.grads->as<R>() + ST_F * last.ld, s);
     launch_axpy_planes<R>(last.n, 3, last.ld, R(1), tmp.as<R>() + 9 * last.ld, last.grads->as<R>() + ST_X * last.ld,
                           s);
@@ -1142,6 +1218,11 @@ void graph_set_up(Graph& G, int num_layers)
 {
     if (num_layers <= 0) fail(MPM_ERR_ARG, "num_layers must be positive");
     cudaStream_t s = G.stream;
+    if (G.resort_on) {
+        // the other layers are rebuilt from layer 0 below: sort layer 0 only
+        G.layers.resize(1);
+        graph_resort<R>(G);
+    }
     G.layers.resize(num_layers);
     for (int i = 1; i < num_layers; ++i) {
         if (G.stored(i)) {
@@ -1758,8 +1839,9 @@ int mpm_compgraph_accumulate_render_grads(mpm_compgraph* cg, const float* dLdF, 
             cudaStream_t s = G.stream;
             ensure_grads(last, s);
             DevBuf tmp((size_t)12 * last.ld * sizeof(R));
-            planes_in<R>(n, 9, last.ld, dLdF, MPM_DTYPE_F32, 0, tmp.as<R>(), s);
-            planes_in<R>(n, 3, last.ld, dLdx, MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s);
+            const int* perm = last.perm ? last.perm->as<int>() : nullptr;
+            planes_in<R>(n, 9, last.ld, dLdF, MPM_DTYPE_F32, 0, tmp.as<R>(), s, perm);
+            planes_in<R>(n, 3, last.ld, dLdx, MPM_DTYPE_F32, 0, tmp.as<R>() + 9 * last.ld, s, perm);
             launch_axpy_planes<R>(n, 9, last.ld, R(1), tmp.as<R>(), last.grads->as<R>() + ST_F * last.ld, s);
             launch_axpy_planes<R>(n, 3, last.ld, R(1), tmp.as<R>() + 9 * last.ld, last.grads->as<R>() + ST_X * last.ld,
                                   s);
@@ -1999,6 +2081,7 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
         T.inst_table = G.inst_table;
         T.total_nodes = G.total_nodes;
         T.stream = s;
+        T.resort_on = false;  // shares G's constant planes: never permute them from here
         T.base = clone_pc(*G.layers[0].pc, s, true);
         T.base->grads.reset();
         T.layers.resize(1);
@@ -2051,6 +2134,22 @@ int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on)
         check_cg(cg);
         cg->g.graphs_on = on != 0;
         if (!on) cg->g.caps.clear();
+    });
+}
+
+int mpm_compgraph_resort(mpm_compgraph* cg)
+{
+    return guard([&] {
+        check_cg(cg);
+        with_prec(cg->g.prec, [&](auto r) { graph_resort<decltype(r)>(cg->g); });
+    });
+}
+
+int mpm_compgraph_set_resort(mpm_compgraph* cg, int on)
+{
+    return guard([&] {
+        check_cg(cg);
+        cg->g.resort_on = on != 0;
     });
 }
 

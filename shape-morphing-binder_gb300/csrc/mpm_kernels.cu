@@ -1712,21 +1712,37 @@ __global__ void __launch_bounds__(kThreads) k_adam(int n, long long ld, const R*
 // ------------------------------------------------------------- utility
 
 template <typename R, typename T>
-__global__ void k_aos_to_planes(int n, int k, long long ld, const T* __restrict__ src, R* __restrict__ dst)
+__global__ void k_aos_to_planes(int n, int k, long long ld, const T* __restrict__ src, R* __restrict__ dst,
+                                const int* __restrict__ perm)
 {
+    // slot p holds the caller's row perm[p] (identity without a permutation)
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * k) return;
-    const int p = (int)(t / k), q = (int)(t % k);
-    dst[(long long)q * ld + p] = (R)src[t];
+    const int p = (int)(t % n), q = (int)(t / n);
+    const long long row = perm ? perm[p] : p;
+    dst[(long long)q * ld + p] = (R)src[row * k + q];
 }
 
 template <typename R, typename T>
-__global__ void k_planes_to_aos(int n, int k, long long ld, const R* __restrict__ src, T* __restrict__ dst)
+__global__ void k_planes_to_aos(int n, int k, long long ld, const R* __restrict__ src, T* __restrict__ dst,
+                                const int* __restrict__ perm)
 {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * k) return;
-    const int p = (int)(t / k), q = (int)(t % k);
-    dst[t] = (T)src[(long long)q * ld + p];
+    const int p = (int)(t % n), q = (int)(t / n);
+    const long long row = perm ? perm[p] : p;
+    dst[row * k + q] = (T)src[(long long)q * ld + p];
+}
+
+// dst slot i <- src slot order[i], plane by plane (the re-sort)
+template <typename R>
+__global__ void k_gather_planes(int n, int k, long long ld, const int* __restrict__ order, const R* __restrict__ src,
+                                R* __restrict__ dst)
+{
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k) return;
+    const int i = (int)(t % n), q = (int)(t / n);
+    dst[(long long)q * ld + i] = src[(long long)q * ld + order[i]];
 }
 
 template <typename R>
@@ -2086,19 +2102,27 @@ void launch_adam(int n, long long ld, const R* gF, R* dfc, double* mom, double* 
 }
 
 template <typename R, typename T>
-void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s)
+void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s, const int* perm)
 {
     if (n <= 0) return;
     counted();
-    k_aos_to_planes<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
+    k_aos_to_planes<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst, perm);
 }
 
 template <typename R, typename T>
-void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s)
+void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s, const int* perm)
 {
     if (n <= 0) return;
     counted();
-    k_planes_to_aos<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst);
+    k_planes_to_aos<R, T><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, src, dst, perm);
+}
+
+template <typename R>
+void launch_gather_planes(int n, int k, long long ld, const int* order, const R* src, R* dst, cudaStream_t s)
+{
+    if (n <= 0) return;
+    counted();
+    k_gather_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, order, src, dst);
 }
 
 template <typename R>
@@ -2150,10 +2174,13 @@ void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStr
     template void launch_sumsq<R>(int, long long, const R*, int, int, double*, cudaStream_t);                     \
     template void launch_adam<R>(int, long long, const R*, R*, double*, double*, double*, double, double, double, \
                                  double, double, int, cudaStream_t);                                               \
-    template void launch_aos_to_planes<R, float>(int, int, long long, const float*, R*, cudaStream_t);            \
-    template void launch_aos_to_planes<R, double>(int, int, long long, const double*, R*, cudaStream_t);          \
-    template void launch_planes_to_aos<R, float>(int, int, long long, const R*, float*, cudaStream_t);            \
-    template void launch_planes_to_aos<R, double>(int, int, long long, const R*, double*, cudaStream_t);          \
+    template void launch_aos_to_planes<R, float>(int, int, long long, const float*, R*, cudaStream_t, const int*); \
+    template void launch_aos_to_planes<R, double>(int, int, long long, const double*, R*, cudaStream_t,           \
+                                                  const int*);                                                      \
+    template void launch_planes_to_aos<R, float>(int, int, long long, const R*, float*, cudaStream_t, const int*); \
+    template void launch_planes_to_aos<R, double>(int, int, long long, const R*, double*, cudaStream_t,           \
+                                                  const int*);                                                      \
+    template void launch_gather_planes<R>(int, int, long long, const int*, const R*, R*, cudaStream_t);           \
     template void launch_axpy_planes<R>(int, int, long long, R, const R*, R*, cudaStream_t);                      \
     template void launch_fill_planes<R>(int, int, long long, R, R*, cudaStream_t);                                \
     template void launch_count_active<R>(const StepCfg&, const R*, unsigned long long*, cudaStream_t);             \

@@ -117,11 +117,26 @@ template <typename R>
 void launch_adam(int n, long long ld, const R* gF, R* dfc, double* mom, double* vec, double* vmax, double alpha,
                  double inv_gn, double beta1, double beta2, double eps, int t, cudaStream_t s);
 
-// layout conversion: (n, k) row-major <-> k planes of stride ld
+// layout conversion: (n, k) row-major <-> k planes of stride ld; with perm,
+// plane slot p holds row perm[p] of the caller's array
 template <typename R, typename T>
-void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s);
+void launch_aos_to_planes(int n, int k, long long ld, const T* src, R* dst, cudaStream_t s,
+                          const int* perm = nullptr);
 template <typename R, typename T>
-void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s);
+void launch_planes_to_aos(int n, int k, long long ld, const R* src, T* dst, cudaStream_t s,
+                          const int* perm = nullptr);
+// k planes: dst slot i <- src slot order[i]
+template <typename R>
+void launch_gather_planes(int n, int k, long long ld, const int* order, const R* src, R* dst, cudaStream_t s);
+
+// Particle order by (instance, grid cell), stable (mpm_sort.cu): order[i] is
+// the slot whose particle moves to slot i.  x: 3 position planes of stride
+// ld, precision R; inst/ninst: the batch (ninst 0: one instance described by
+// c's grid).  Padding slots of a batch stay at the end of their instance.
+// false: scratch allocation or sort failed (order not written).
+template <typename R>
+bool cell_order(const StepCfg& c, const InstHost* inst, int ninst, int n, long long ld, const R* x, int* order,
+                cudaStream_t s);
 template <typename R>
 void launch_axpy_planes(int n, int k, long long ld, R alpha, const R* x, R* y, cudaStream_t s);
 template <typename R>

@@ -372,6 +372,15 @@ class CompGraph:
         return dict(precision=o.precision, adjoint=o.adjoint, kernel=o.kernel, material=o.material,
                     checkpoint_every=o.checkpoint_every, deterministic=bool(o.deterministic))
 
+    def resort(self):
+        """Order the particles by grid cell (additive; the order callers see
+        does not change)."""
+        check(lib.mpm_compgraph_resort(self._h))
+
+    def set_resort(self, on=True):
+        """Re-sort at set_up_comp_graph (default on)."""
+        check(lib.mpm_compgraph_set_resort(self._h, int(bool(on))))
+
     def set_deterministic(self, on=True):
         """Fixed-point node sums (FP32 graphs): bitwise reproducible passes."""
         check(lib.mpm_compgraph_set_deterministic(self._h, int(bool(on))))

@@ -124,11 +124,12 @@ def test_unsorted_particles(dm, orc):
     sp = O.State(s0.x[perm], s0.v[perm], s0.C[perm], s0.F[perm], s0.m[perm], s0.vol[perm], s0.lam[perm],
                  s0.mu[perm], s0.dFc[perm])
     prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
-    cg, keep = make_graph(dm, sp, g, prm, precision="fp32")
-    cg.compute_forward_pass(0, 0)
-    want, _ = orc.forward_step(g, prm, sp)
-    got = layer_state(cg, 1)
-    assert rel_err(got["x"], want.x) < 1e-6 and rel_err(got["C"], want.C) < 1e-4
+    for resort in (False, True):  # shuffled slots, and re-sorted by cell behind the caller's order
+        cg, keep = make_graph(dm, sp, g, prm, precision="fp32", layers=2, resort=resort)
+        cg.compute_forward_pass(0, 0)
+        want, _ = orc.forward_step(g, prm, sp)
+        got = layer_state(cg, 1)
+        assert rel_err(got["x"], want.x) < 1e-6 and rel_err(got["C"], want.C) < 1e-4
 
 
 @pytest.mark.parametrize("kernel,material", [("quadratic", "fcr"), ("cubic", "neohookean"), ("quadratic", "neohookean")])
