@@ -32,6 +32,9 @@ namespace mpm {
 #ifndef MPM_P2G_ADJ_MIN_BLOCKS
 #define MPM_P2G_ADJ_MIN_BLOCKS 1
 #endif
+#ifndef MPM_G2P_MIN_BLOCKS
+#define MPM_G2P_MIN_BLOCKS 3
+#endif
 
 int g_tile_nodes = 2048;
 int g_scatter_mode = 1;
@@ -786,7 +789,7 @@ MPM_D void g2p_finish(const KP<R>& kp, long long ld, int p, const R* x, const R*
 }
 
 template <typename R, int K>
-__global__ void __launch_bounds__(kThreads) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+__global__ void __launch_bounds__(kThreads, MPM_G2P_MIN_BLOCKS) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
                                                    const R* __restrict__ dfc, const R* __restrict__ grid,
                                                    R* __restrict__ st1, R* __restrict__ trust)
 {
