@@ -153,6 +153,15 @@ int mpm_grid_release(mpm_grid* g);
 int mpm_p2g(mpm_pointcloud* pc, mpm_grid* g);
 /* CalculatePointCloudVolumes (ForwardSimulation.cpp:234-271; bind.cpp:551-554) */
 int mpm_calculate_point_cloud_volumes(mpm_pointcloud* pc, mpm_grid* g);
+/* The inside test of GeometryLoading::GeneratePointCloudFromWatertightTriangleMesh
+ * (GeometryLoading.cpp:57-77, libigl signed distance under the winding-number
+ * sign; reached from load_point_cloud_from_obj, bind.cpp:531-538): the
+ * generalized winding number of n_points points (n,3) w.r.t. n_tris
+ * triangles given by their vertices (n_tris,3,3), into out (n doubles).
+ * Points on the surface get exactly 0.5; |w| >= 0.5 is inside.  on_device:
+ * the three arrays are device pointers (else host pointers). */
+int mpm_winding_numbers(int n_points, const float* points, int n_tris, const float* tri_vertices, double* out,
+                        int on_device, void* stream);
 
 /* -------------------------------------------------------------- CompGraph */
 /* CompGraph(pc, grid, target_grid) (CompGraph.cpp:21-28; bind.cpp:163-164):

@@ -31,6 +31,7 @@ REF_DIR = Path(os.environ.get("REF_DIR", "/root/reference"))
 REF_SOURCES = [
     "ForwardSimulation.cpp", "BackPropagation.cpp", "Elasticity.cpp", "PointCloud.cpp",
     "Grid.cpp", "GridNode.cpp", "MaterialPoint.cpp", "CompGraph.cpp", "Tensor3x3x3x3.cpp",
+    "GeometryLoading.cpp",  # mesh -> lattice sampling (libigl signed distance, header-only)
 ]
 CXXFLAGS = ["-std=c++17", "-O2", "-fopenmp", "-fPIC", "-fno-fast-math", "-ffp-contract=off",
             "-DNDEBUG", "-DEIGEN_NO_DEBUG", "-D_USE_MATH_DEFINES", "-w"]

@@ -458,3 +458,17 @@ class Reference:
                                      C.c_int(max_ls_iters), C.c_double(initial_alpha), C.c_double(gd_tol),
                                      _p(dfc), _p(xT), log, C.c_int(len(log)))
         return loss, dfc, xT, log.value.decode(errors="replace")
+
+    def sample_mesh(self, V, F, dx: float):
+        """GeneratePointCloudFromWatertightTriangleMesh over the mesh's bounding
+        box (the reference's lattice + libigl winding-number inside test)."""
+        V = np.ascontiguousarray(V, np.float64).reshape(-1, 3)
+        Fi = np.ascontiguousarray(F, np.int32).reshape(-1, 3)
+        cap = 1
+        for d in range(3):
+            cap *= int(np.ceil((V[:, d].max() - V[:, d].min()) / dx)) + 2
+        out = np.zeros((cap, 3))
+        self.lib.ref_sample_mesh.restype = C.c_int
+        k = self.lib.ref_sample_mesh(_p(V), C.c_int(len(V)), Fi.ctypes.data_as(_ip), C.c_int(len(Fi)),
+                                     C.c_double(dx), _p(out), C.c_int(cap))
+        return out[:min(k, cap)]

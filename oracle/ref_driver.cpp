@@ -17,6 +17,7 @@
 #include "BackPropagation.h"
 #include "CompGraph.h"
 #include "Elasticity.h"
+#include "GeometryLoading.h"
 
 #include <cstdio>
 #include <cstring>
@@ -311,6 +312,31 @@ double ref_optimize(const int* dims, double dx, const double* mn, double dt, dou
         for (int p = 0; p < n; ++p) put(cg.layers[l].point_cloud->points[p].dFc, dFc_out + (l * n + p) * 9);
     for (int p = 0; p < n; ++p) put(cg.layers.back().point_cloud->points[p].x, xT + 3 * p);
     return loss;
+}
+
+// GeneratePointCloudFromWatertightTriangleMesh (GeometryLoading.cpp:10-83)
+// over the mesh's bounding box, as LoadMPMPointCloudFromObj calls it
+// (GeometryLoading.cpp:103-118): writes up to cap points (cap,3) and returns
+// how many the reference keeps.
+int ref_sample_mesh(const double* V, int nv, const int* F, int nt, double dx, double* out, int cap)
+{
+    Eigen::Matrix<Real, Eigen::Dynamic, Eigen::Dynamic> Vm(nv, 3);
+    Eigen::MatrixXi Fm(nt, 3);
+    for (int i = 0; i < nv; ++i)
+        for (int j = 0; j < 3; ++j) Vm(i, j) = (Real)V[3 * i + j];
+    for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < 3; ++j) Fm(i, j) = F[3 * i + j];
+    Vec3 mn, mx;
+    for (int j = 0; j < 3; ++j) {
+        mn[j] = Vm.col(j).minCoeff();
+        mx[j] = Vm.col(j).maxCoeff();
+    }
+    std::streambuf* old = std::cout.rdbuf(nullptr);
+    std::vector<Vec3> pts = GeometryLoading::GeneratePointCloudFromWatertightTriangleMesh(Vm, Fm, mn, mx, (Real)dx);
+    std::cout.rdbuf(old);
+    const int k = (int)std::min<size_t>(pts.size(), (size_t)cap);
+    for (int i = 0; i < k; ++i) put(pts[i], out + 3 * i);
+    return (int)pts.size();
 }
 
 }  // extern "C"

@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 INCLUDE = HERE.parent / "include"
 LIB = HERE / "diffmpm_bindings" / "libmpm.so"
-SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu", "mpm_geometry.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

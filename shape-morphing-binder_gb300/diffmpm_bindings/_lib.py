@@ -100,6 +100,7 @@ _SIGS = {
     "mpm_compgraph_set_tuning": [_vp, C.c_int, C.c_int],
     "mpm_compgraph_set_deterministic": [_vp, C.c_int],
     "mpm_compgraph_resort": [_vp],
+    "mpm_winding_numbers": [C.c_int, _vp, C.c_int, _vp, _vp, C.c_int, _vp],
     "mpm_compgraph_set_resort": [_vp, C.c_int],
     "mpm_compgraph_loss_history": [_vp, _dp, C.c_int, _ip],
     "mpm_step_count": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],

@@ -1,16 +1,21 @@
-"""Mesh -> particle lattice sampling (setup time, host side).
+"""Mesh -> particle lattice sampling (setup time).
 
 Restates GeometryLoading::LoadMPMPointCloudFromObj (GeometryLoading.cpp:85-143):
 a lattice of spacing ``point_dx`` over the mesh's bounding box
 (dims = ceil((max - min) / dx) + 1, k fastest), keeping the lattice points
 inside the mesh.  The reference classifies points with libigl's signed
-distance under the winding-number sign; here the inside test is the
-generalized winding number (sum of signed solid angles / 4 pi >= 1/2), with
-the solid angle of each triangle from the Van Oosterom-Strackee formula.
+distance under the winding-number sign (GeometryLoading.cpp:57-77); here the
+inside test is the generalized winding number computed on the GPU
+(``mpm_winding_numbers``: |w| >= 1/2 inside, points on the surface kept).
+OBJ parsing and the lattice are host work.
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
+
+from . import _lib
 
 
 def read_obj(path: str):
@@ -30,20 +35,15 @@ def read_obj(path: str):
     return np.asarray(verts, np.float32), np.asarray(faces, np.int64)
 
 
-def winding_numbers(points: np.ndarray, V: np.ndarray, F: np.ndarray, chunk: int = 1 << 22) -> np.ndarray:
-    """Generalized winding number of each point w.r.t. the triangle soup (V, F)."""
-    P = np.asarray(points, np.float64)
-    T = np.asarray(V, np.float64)[F]  # (t,3,3)
+def winding_numbers(points: np.ndarray, V: np.ndarray, F: np.ndarray) -> np.ndarray:
+    """Generalized winding number of each point w.r.t. the triangle mesh (V, F),
+    computed on the GPU (points on the surface: exactly 0.5)."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    T = np.ascontiguousarray(np.asarray(V, np.float32)[np.asarray(F, np.int64)]).reshape(-1, 9)
     out = np.zeros(len(P))
-    step = max(1, chunk // max(1, len(T)))
-    for s in range(0, len(P), step):
-        p = P[s:s + step, None, None, :]
-        a, b, c = T[None, :, 0] - p[:, :, 0], T[None, :, 1] - p[:, :, 0], T[None, :, 2] - p[:, :, 0]
-        la, lb, lc = (np.linalg.norm(u, axis=-1) for u in (a, b, c))
-        num = np.einsum("ptk,ptk->pt", a, np.cross(b, c))
-        den = la * lb * lc + np.einsum("ptk,ptk->pt", a, b) * lc + np.einsum("ptk,ptk->pt", a, c) * lb + \
-            np.einsum("ptk,ptk->pt", b, c) * la
-        out[s:s + step] = (2.0 * np.arctan2(num, den)).sum(axis=1) / (4.0 * np.pi)
+    _lib.check(_lib.lib.mpm_winding_numbers(len(P), P.ctypes.data_as(C.c_void_p), len(T),
+                                            T.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p), 0, None),
+               "winding_numbers")
     return out
 
 

@@ -6,11 +6,13 @@ the reference's ForwardTimeStep, Back_Timestep, EndLayerMassLoss,
 Descend_Adam, CalculatePointCloudVolumes, PK_FixedCorotatedElasticity and
 d2_FCE_psi_dF2_mult_by_dF, plus a 5-step full-tape forward/backward through
 CompGraph (reference_small.npz), and a run of the control-sequence
-optimiser OptimizeDefGradControlSequence (reference_optimize.npz).  The
+optimiser OptimizeDefGradControlSequence (reference_optimize.npz) and the
+mesh -> lattice sampler GeneratePointCloudFromWatertightTriangleMesh on two
+procedural meshes (reference_mesh_sampling.npz).  The
 fixtures travel with the repository; the GPU tests compare against them
 without the reference present.
 
-Usage: python tests/golden/make_golden.py [--only small|optimize]
+Usage: python tests/golden/make_golden.py [--only small|optimize|mesh]
 """
 from __future__ import annotations
 
@@ -39,6 +41,60 @@ def small_state(seed=7, G=10, rng_scale=1.0):
     dFc = 0.01 * rng.normal(size=(n, 3, 3))
     s = O.State(w.x, w.v, C0, F0, w.m, w.vol, w.lam, w.mu, dFc)
     return w, s, rng
+
+
+def uv_ellipsoid(c=(0.5, 0.5, 0.5), axes=(0.3, 0.22, 0.18), nu=48, nv=24):
+    """Closed triangle mesh of an ellipsoid (poles + rings), outward facing."""
+    c, a = np.asarray(c), np.asarray(axes)
+    V = [c + a * [0, 0, 1]]
+    for i in range(1, nv):
+        th = np.pi * i / nv
+        for j in range(nu):
+            ph = 2 * np.pi * j / nu
+            V.append(c + a * [np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+    V.append(c + a * [0, 0, -1])
+    F = []
+    ring = lambda i, j: 1 + (i - 1) * nu + (j % nu)  # noqa: E731
+    for j in range(nu):
+        F.append([0, ring(1, j), ring(1, j + 1)])
+    for i in range(1, nv - 1):
+        for j in range(nu):
+            F.append([ring(i, j), ring(i + 1, j), ring(i + 1, j + 1)])
+            F.append([ring(i, j), ring(i + 1, j + 1), ring(i, j + 1)])
+    last = len(V) - 1
+    for j in range(nu):
+        F.append([last, ring(nv - 1, j + 1), ring(nv - 1, j)])
+    return np.asarray(V, np.float32), np.asarray(F, np.int32)
+
+
+def torus(c=(0.5, 0.5, 0.5), R=0.25, r=0.1, nu=48, nv=24):
+    """Closed triangle mesh of a torus around z (non-convex)."""
+    c = np.asarray(c)
+    V = []
+    for i in range(nu):
+        u = 2 * np.pi * i / nu
+        for j in range(nv):
+            v = 2 * np.pi * j / nv
+            V.append(c + [(R + r * np.cos(v)) * np.cos(u), (R + r * np.cos(v)) * np.sin(u), r * np.sin(v)])
+    idx = lambda i, j: (i % nu) * nv + (j % nv)  # noqa: E731
+    F = []
+    for i in range(nu):
+        for j in range(nv):
+            F.append([idx(i, j), idx(i + 1, j), idx(i + 1, j + 1)])
+            F.append([idx(i, j), idx(i + 1, j + 1), idx(i, j + 1)])
+    return np.asarray(V, np.float32), np.asarray(F, np.int32)
+
+
+def make_mesh_sampling():
+    """The reference's mesh -> lattice sampler on two procedural meshes."""
+    r32 = O.Reference(32)
+    rec = {}
+    for name, (V, F), dx in (("ellipsoid", uv_ellipsoid(), 1.0 / 48), ("torus", torus(), 1.0 / 64)):
+        pts = r32.sample_mesh(V, F, dx)
+        rec[f"{name}_V"], rec[f"{name}_F"], rec[f"{name}_dx"], rec[f"{name}_points"] = V, F, dx, pts
+        print(name, "triangles", len(F), "points kept", len(pts))
+    np.savez_compressed(OUT / "reference_mesh_sampling.npz", **rec)
+    print("wrote", OUT / "reference_mesh_sampling.npz")
 
 
 OPT_CASE = dict(num_steps=6, control_stride=2, max_gd_iters=2, max_ls_iters=4, initial_alpha=0.05, gd_tol=1e-4)
@@ -73,13 +129,15 @@ def make_optimize():
     print("wrote", OUT / "reference_optimize.npz", "N =", s.n)
 
 
-def main(which=("small", "optimize")):
+def main(which=("small", "optimize", "mesh")):
     build_oracle.build_oracle()
     outs = build_oracle.build_ref()
     if not outs:
         raise SystemExit("reference tree not found; golden vectors need the reference sources")
     if "optimize" in which:
         make_optimize()
+    if "mesh" in which:
+        make_mesh_sampling()
     if "small" not in which:
         return
     r64, r32 = O.Reference(64), O.Reference(32)
@@ -157,6 +215,6 @@ def main(which=("small", "optimize")):
 if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["small", "optimize"])
+    ap.add_argument("--only", choices=["small", "optimize", "mesh"])
     a = ap.parse_args()
-    main((a.only,) if a.only else ("small", "optimize"))
+    main((a.only,) if a.only else ("small", "optimize", "mesh"))

