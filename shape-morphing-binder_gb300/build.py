@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 INCLUDE = HERE.parent / "include"
 LIB = HERE / "diffmpm_bindings" / "libmpm.so"
-SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu", "mpm_geometry.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu", "mpm_geometry.cu", "gs_rasterizer.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,7 +36,7 @@ def flags(debug: bool = False):
 
 def _inputs():
     return [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + \
-        [INCLUDE / "mpm.h", Path(__file__)]
+        [INCLUDE / "mpm.h", INCLUDE / "gsplat.h", Path(__file__)]
 
 
 def up_to_date() -> bool:

@@ -101,6 +101,11 @@ _SIGS = {
     "mpm_compgraph_set_deterministic": [_vp, C.c_int],
     "mpm_compgraph_resort": [_vp],
     "mpm_winding_numbers": [C.c_int, _vp, C.c_int, _vp, _vp, C.c_int, _vp],
+    # Gaussian-splatting rasterizer (include/gsplat.h; structs passed by pointer)
+    "gs_scratch_bytes": [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],
+    "gs_preprocess": [_vp, _vp, _vp, C.c_size_t, _ip, _vp],
+    "gs_render": [_vp, _vp, C.c_int, _vp, _vp, C.c_size_t, _vp, _vp],
+    "gs_backward": [_vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "mpm_compgraph_set_resort": [_vp, C.c_int],
     "mpm_compgraph_loss_history": [_vp, _dp, C.c_int, _ip],
     "mpm_step_count": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],

@@ -1,0 +1,178 @@
+"""Dense PyTorch reference of the Gaussian rasterizer (TEST INFRASTRUCTURE).
+
+The same forward as the sm_103a kernels (the reference's diff_gauss
+semantics, forward.cu:204-455): near culling at view z <= 0.2, EWA 2D
+covariance at the 1.3 x FOV clamped view point plus the 0.3 px low-pass,
+3-sigma radius and 16 x 16 tile rectangle, SH or precomputed color clamped
+at 0, normals from the smallest-scale axis facing the camera, per-tile depth
+order, alpha = min(0.99, o exp(power)) with power > 0 and alpha < 1/255
+skipped, and a pixel stopping before its transmittance drops below 1e-4.
+Every pixel is evaluated against every Gaussian in float64 (no tiles), so
+torch autograd gives the exact gradient to compare the hand-written adjoint
+with.  Small scenes only.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+Y0 = 0.28209479177387814
+Y1 = 0.4886025119029199
+Y2 = [1.0925484305920792, -1.0925484305920792, 0.31539156525252005, -1.0925484305920792, 0.5462742152960396]
+Y3 = [-0.5900435899266435, 2.890611442640554, -0.4570457994644658, 0.3731763325901154, -0.4570457994644658,
+      1.445305721320277, -0.5900435899266435]
+
+
+def sh_basis(deg, d):
+    x, y, z = d[:, 0], d[:, 1], d[:, 2]
+    b = [torch.full_like(x, Y0)]
+    if deg >= 1:
+        b += [-Y1 * y, Y1 * z, -Y1 * x]
+    if deg >= 2:
+        xx, yy, zz = x * x, y * y, z * z
+        b += [Y2[0] * x * y, Y2[1] * y * z, Y2[2] * (2 * zz - xx - yy), Y2[3] * x * z, Y2[4] * (xx - yy)]
+    if deg >= 3:
+        b += [Y3[0] * y * (3 * xx - yy), Y3[1] * x * y * z, Y3[2] * y * (4 * zz - xx - yy),
+              Y3[3] * z * (2 * zz - 3 * xx - 3 * yy), Y3[4] * x * (4 * zz - xx - yy), Y3[5] * z * (xx - yy),
+              Y3[6] * x * (xx - 3 * yy)]
+    return torch.stack(b, 1)  # (P, nb)
+
+
+def quat_rot(q):
+    r, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - r * z), 2 * (x * z + r * y),
+                        2 * (x * y + r * z), 1 - 2 * (x * x + z * z), 2 * (y * z - r * x),
+                        2 * (x * z - r * y), 2 * (y * z + r * x), 1 - 2 * (x * x + y * y)], 1).reshape(-1, 3, 3)
+
+
+def render(means3D, opacities, H, W, tanfovx, tanfovy, bg, view, proj, campos, *, colors=None, shs=None,
+           sh_degree=0, scales=None, rotations=None, cov3D=None, norm3D=None, extra=None, scale_modifier=1.0,
+           ndc_out=None):
+    """(color (3,H,W), depth (1,H,W), normal (3,H,W) not normalised, alpha (1,H,W), radii (P,), extra).
+    ndc_out: a list that receives the projected means (P,3) with retain_grad (the
+    means2D gradient the rasterizer reports is the gradient w.r.t. its x, y)."""
+    dt = torch.float64
+    m = means3D.to(dt)
+    P = m.shape[0]
+    V = view.to(dt).reshape(4, 4)
+    Pm = proj.to(dt).reshape(4, 4)
+    t = m @ V[:3, :3] + V[3, :3]
+    ph = m @ Pm[:3] + Pm[3]
+    pp = ph[:, :3] / (ph[:, 3:4] + 1e-7)
+    if ndc_out is not None:
+        pp.retain_grad()
+        ndc_out.append(pp)
+    if cov3D is not None:
+        c = cov3D.to(dt)
+        S = torch.stack([c[:, 0], c[:, 1], c[:, 2], c[:, 1], c[:, 3], c[:, 4], c[:, 2], c[:, 4], c[:, 5]],
+                        1).reshape(-1, 3, 3)
+    else:
+        R = quat_rot(rotations.to(dt))
+        M = (scale_modifier * scales.to(dt))[:, :, None] * R
+        S = M.transpose(1, 2) @ M
+    if norm3D is not None:
+        nrm = norm3D.to(dt)
+    else:
+        R = quat_rot(rotations.to(dt))
+        s = scales
+        axis = torch.where((s[:, 0] > s[:, 2]) & (s[:, 1] > s[:, 2]), 2,
+                           torch.where((s[:, 0] > s[:, 1]) & (s[:, 2] > s[:, 1]), 1, 0))
+        nrm = R[torch.arange(P), axis]
+        ray = m - campos.to(dt)
+        flip = ((ray * nrm).sum(1) > 0).to(dt)
+        nrm = nrm * (1 - 2 * flip)[:, None]
+    fx, fy = W / (2 * tanfovx), H / (2 * tanfovy)
+    limx, limy = 1.3 * tanfovx, 1.3 * tanfovy
+    tx = torch.clamp(t[:, 0] / t[:, 2], -limx, limx) * t[:, 2]
+    ty = torch.clamp(t[:, 1] / t[:, 2], -limy, limy) * t[:, 2]
+    tz = t[:, 2]
+    zero = torch.zeros_like(tz)
+    J = torch.stack([fx / tz, zero, -fx * tx / tz ** 2, zero, fy / tz, -fy * ty / tz ** 2], 1).reshape(-1, 2, 3)
+    U = J @ V[:3, :3].T
+    cov2 = U @ S @ U.transpose(1, 2) + 0.3 * torch.eye(2, dtype=dt)
+    a, b, cc = cov2[:, 0, 0], cov2[:, 0, 1], cov2[:, 1, 1]
+    det = a * cc - b * b
+    conic = torch.stack([cc / det, -b / det, a / det], 1)
+    with torch.no_grad():
+        mid = 0.5 * (a + cc)
+        l1 = mid + torch.sqrt(torch.clamp(mid * mid - det, min=0.1))
+        l2 = mid - torch.sqrt(torch.clamp(mid * mid - det, min=0.1))
+        radius = torch.ceil(3 * torch.sqrt(torch.maximum(l1, l2)))
+    px = ((pp[:, 0] + 1) * W - 1) * 0.5
+    py = ((pp[:, 1] + 1) * H - 1) * 0.5
+    gx, gy = (W + 15) // 16, (H + 15) // 16
+    with torch.no_grad():
+        r = radius
+        x0 = torch.clamp(torch.trunc((px - r) / 16), 0, gx).long()
+        y0 = torch.clamp(torch.trunc((py - r) / 16), 0, gy).long()
+        x1 = torch.clamp(torch.trunc((px + r + 15) / 16), 0, gx).long()
+        y1 = torch.clamp(torch.trunc((py + r + 15) / 16), 0, gy).long()
+        keep = (tz > 0.2) & (det != 0) & ((x1 - x0) * (y1 - y0) > 0)
+    if colors is not None:
+        rgb = colors.to(dt)
+    else:
+        d = m - campos.to(dt)
+        d = d / d.norm(dim=1, keepdim=True)
+        nb = (sh_degree + 1) ** 2
+        rgb = torch.clamp_min((sh_basis(sh_degree, d)[:, :, None] * shs.to(dt)[:, :nb]).sum(1) + 0.5, 0.0)
+    ED = 0 if extra is None else extra.shape[1]
+    # pixels
+    yy, xx = torch.meshgrid(torch.arange(H, dtype=dt), torch.arange(W, dtype=dt), indexing="ij")
+    pxf, pyf = xx.reshape(-1), yy.reshape(-1)
+    ptx, pty = (pxf // 16).long(), (pyf // 16).long()
+    order = torch.argsort(tz.detach(), stable=True)
+    T = torch.ones_like(pxf)
+    Cc = torch.zeros((3, H * W), dtype=dt)
+    D = torch.zeros(H * W, dtype=dt)
+    N = torch.zeros((3, H * W), dtype=dt)
+    E = torch.zeros((ED, H * W), dtype=dt)
+    done = torch.zeros(H * W, dtype=torch.bool)
+    op = opacities.to(dt).reshape(-1)
+    for i in order.tolist():
+        if not bool(keep[i]):
+            continue
+        in_tile = (ptx >= x0[i]) & (ptx < x1[i]) & (pty >= y0[i]) & (pty < y1[i]) & ~done
+        dx, dy = px[i] - pxf, py[i] - pyf
+        power = -0.5 * (conic[i, 0] * dx * dx + conic[i, 2] * dy * dy) - conic[i, 1] * dx * dy
+        alpha = torch.clamp_max(op[i] * torch.exp(power), 0.99)
+        use = in_tile & (power <= 0) & (alpha >= 1.0 / 255.0)
+        nT = T * (1 - alpha)
+        stop = use & (nT < 0.0001)
+        done = done | stop
+        use = use & ~stop
+        w = torch.where(use, alpha * T, torch.zeros_like(T))
+        Cc = Cc + rgb[i][:, None] * w[None]
+        D = D + t[i, 2] * w
+        N = N + nrm[i][:, None] * w[None]
+        if ED:
+            E = E + extra[i].to(dt)[:, None] * w[None]
+        T = torch.where(use, nT, T)
+    color = (Cc + T[None] * bg.to(dt)[:, None]).reshape(3, H, W)
+    radii = torch.where(keep, radius, torch.zeros_like(radius)).to(torch.int32)
+    return color, D.reshape(1, H, W), N.reshape(3, H, W), (1 - T).reshape(1, H, W), radii, E.reshape(ED, H, W)
+
+
+def camera(H, W, fovx_deg=50.0, eye=(0.0, 0.0, -3.0), target=(0.0, 0.0, 0.0), znear=0.01, zfar=100.0):
+    """World-to-view and full projection matrices in the rasterizer's flat
+    convention (x' = m[0]x + m[4]y + m[8]z + m[12]): a look-at camera."""
+    tanx = math.tan(math.radians(fovx_deg) / 2)
+    tany = tanx * H / W
+    eye_t, tgt = torch.tensor(eye, dtype=torch.float64), torch.tensor(target, dtype=torch.float64)
+    fwd = tgt - eye_t
+    fwd = fwd / fwd.norm()
+    up = torch.tensor([0.0, 1.0, 0.0], dtype=torch.float64)
+    right = torch.cross(up, fwd, dim=0)
+    right = right / right.norm()
+    up2 = torch.cross(fwd, right, dim=0)
+    Rw = torch.stack([right, up2, fwd])            # rows: camera axes in world
+    tw = -Rw @ eye_t
+    Wv = torch.eye(4, dtype=torch.float64)
+    Wv[:3, :3], Wv[:3, 3] = Rw, tw                  # column-vector world->view
+    Pr = torch.zeros(4, 4, dtype=torch.float64)
+    Pr[0, 0], Pr[1, 1] = 1 / tanx, 1 / tany
+    Pr[2, 2], Pr[2, 3] = zfar / (zfar - znear), -zfar * znear / (zfar - znear)
+    Pr[3, 2] = 1.0
+    view = Wv.T.contiguous().reshape(-1)            # flat layout m[4c+r] = Wv[r][c]
+    proj = (Pr @ Wv).T.contiguous().reshape(-1)
+    return tanx, tany, view, proj, eye_t

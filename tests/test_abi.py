@@ -1,4 +1,4 @@
-"""libmpm.so loads and exports every entry point include/mpm.h declares
+"""libmpm.so loads and exports every entry point include/*.h declares
 (no compute calls: this runs without a GPU)."""
 import ctypes
 import re
@@ -8,9 +8,11 @@ ROOT = Path(__file__).resolve().parents[1]
 
 
 def declared_functions():
-    text = (ROOT / "include" / "mpm.h").read_text()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(mpm_[a-z0-9_]+)\s*\(", text)))
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b((?:mpm|gs)_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_entry_points():

@@ -1,0 +1,177 @@
+"""The sm_103a Gaussian rasterizer (diff_gauss module, include/gsplat.h)
+against a dense float64 PyTorch evaluation of the same operation
+(tests/gs_reference.py): forward outputs (color, depth, normal, alpha,
+radii, extra channels) and, through torch autograd of the dense reference,
+the gradients of every input the reference's diff_gauss differentiates
+(means3D, means2D, SH or precomputed colors, opacities, scales, rotations,
+precomputed covariance and normals, extra attributes).
+
+Tolerances: forward 1e-4 (absolute, FP32 against FP64); gradients 2e-3
+relative in norm (FP32 per-pixel terms summed with warp reductions and
+atomics, in a different order from the dense sum)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _scene(seed, P=150, H=40, W=56, sh_degree=None, extra=0):
+    import gs_reference as R
+    g = torch.Generator().manual_seed(seed)
+    d = torch.float64
+    tanx, tany, view, proj, eye = R.camera(H, W, fovx_deg=55.0)
+    m = (torch.rand(P, 3, generator=g, dtype=d) - 0.5) * torch.tensor([2.0, 1.6, 1.5], dtype=d)
+    sc = 0.02 + 0.12 * torch.rand(P, 3, generator=g, dtype=d)
+    q = torch.randn(P, 4, generator=g, dtype=d)
+    q = q / q.norm(dim=1, keepdim=True)
+    op = 0.1 + 0.85 * torch.rand(P, 1, generator=g, dtype=d)
+    out = dict(means3D=m, scales=sc, rotations=q, opacities=op, H=H, W=W, tanx=tanx, tany=tany, view=view,
+               proj=proj, campos=eye, bg=torch.tensor([0.2, 0.4, 0.7], dtype=d))
+    if sh_degree is None:
+        out["colors"] = torch.rand(P, 3, generator=g, dtype=d)
+    else:
+        out["shs"] = 0.4 * torch.randn(P, 16, 3, generator=g, dtype=d)
+        out["sh_degree"] = sh_degree
+    if extra:
+        out["extra"] = torch.randn(P, extra, generator=g, dtype=d)
+    return out
+
+
+def _ours(dm, sc, dev, cov3D=None, norm3D=None, leaf=True):
+    import diff_gauss as dg
+    t = lambda x: x.to(dev, torch.float32).clone().requires_grad_(leaf)  # noqa: E731
+    ins = {k: t(sc[k]) for k in ("means3D", "opacities", "scales", "rotations", "colors", "shs", "extra") if k in sc}
+    means2D = torch.zeros_like(ins["means3D"], requires_grad=True)
+    st = dg.GaussianRasterizationSettings(
+        image_height=sc["H"], image_width=sc["W"], tanfovx=sc["tanx"], tanfovy=sc["tany"],
+        bg=sc["bg"].to(dev, torch.float32), scale_modifier=1.0, viewmatrix=sc["view"].to(dev, torch.float32),
+        projmatrix=sc["proj"].to(dev, torch.float32), sh_degree=sc.get("sh_degree", 0),
+        campos=sc["campos"].to(dev, torch.float32), prefiltered=False, debug=False)
+    empty = torch.empty(0, device=dev)
+    out = dg.rasterize_gaussians(ins["means3D"], means2D, ins.get("shs", empty), ins.get("colors", empty),
+                                 ins["opacities"], ins["scales"] if cov3D is None else empty,
+                                 ins["rotations"] if cov3D is None else empty,
+                                 empty if cov3D is None else cov3D, empty if norm3D is None else norm3D,
+                                 ins.get("extra", empty), st)
+    return out, ins, means2D
+
+
+def _reference(sc, cov3D=None, norm3D=None):
+    import gs_reference as R
+    ins = {k: sc[k].clone().requires_grad_(True) for k in
+           ("means3D", "opacities", "scales", "rotations", "colors", "shs", "extra") if k in sc}
+    ndc = []
+    out = R.render(ins["means3D"], ins["opacities"], sc["H"], sc["W"], sc["tanx"], sc["tany"], sc["bg"], sc["view"],
+                   sc["proj"], sc["campos"], colors=ins.get("colors"), shs=ins.get("shs"),
+                   sh_degree=sc.get("sh_degree", 0), scales=None if cov3D is not None else ins["scales"],
+                   rotations=None if cov3D is not None else ins["rotations"], cov3D=cov3D, norm3D=norm3D,
+                   extra=ins.get("extra"), ndc_out=ndc)
+    color, depth, nrm, alpha, radii, extra = out
+    nrm = torch.nn.functional.normalize(nrm, p=2, dim=0)
+    return (color, depth, nrm, alpha, radii, extra), ins, ndc[0]
+
+
+def _loss(out, w):
+    color, depth, nrm, alpha, _, extra = out
+    l = (color * w["c"]).sum() + 0.1 * (depth * w["d"]).sum() + (nrm * w["n"]).sum() + (alpha * w["a"]).sum()
+    if extra.numel():
+        l = l + (extra * w["e"][: extra.shape[0]]).sum()
+    return l
+
+
+def _weights(H, W, seed=5):
+    g = torch.Generator().manual_seed(seed)
+    d = torch.float64
+    return dict(c=torch.randn(3, H, W, generator=g, dtype=d), d=torch.randn(1, H, W, generator=g, dtype=d),
+                n=torch.randn(3, H, W, generator=g, dtype=d), a=torch.randn(1, H, W, generator=g, dtype=d),
+                e=torch.randn(8, H, W, generator=g, dtype=d))
+
+
+def _close(a, b, atol):
+    a = a.detach().double().cpu()
+    b = b.detach().double().cpu()
+    return float((a - b).abs().max())
+
+
+def _rel(a, b):
+    a = a.detach().double().cpu()
+    b = b.detach().double().cpu()
+    return float((a - b).norm() / max(float(b.norm()), 1e-30))
+
+
+@pytest.mark.parametrize("sh_degree,extra", [(None, 0), (None, 5), (0, 0), (1, 0), (3, 3)])
+def test_forward_and_gradients_match_dense_reference(dm, sh_degree, extra):
+    dev = torch.device("cuda")
+    sc = _scene(3 + (sh_degree or 0), sh_degree=sh_degree, extra=extra)
+    out, ins, m2 = _ours(dm, sc, dev)
+    ref, rins, ndc = _reference(sc)
+    assert torch.equal(out[4].cpu(), ref[4])  # radii
+    assert int((ref[4] > 0).sum()) > 100
+    for k, name in enumerate(("color", "depth", "normal", "alpha")):
+        err = _close(out[k], ref[k], 1e-4)
+        assert err < (5e-4 if name == "depth" else 1e-4), (name, err)
+    if extra:
+        assert _close(out[5], ref[5], 1e-4) < 1e-4
+    w = _weights(sc["H"], sc["W"])
+    _loss(out, {k: v.to(dev, torch.float32) for k, v in w.items()}).backward()
+    _loss(ref, w).backward()
+    for k in rins:
+        e = _rel(ins[k].grad, rins[k].grad)
+        print(f"sh={sh_degree} extra={extra} grad {k}: {e:.2e}")
+        assert e < 2e-3, (k, e)
+    e2 = _rel(m2.grad[:, :2], ndc.grad[:, :2])
+    assert e2 < 2e-3, e2
+
+
+def test_precomputed_covariance_and_normals(dm):
+    import gs_reference as R
+    dev = torch.device("cuda")
+    sc = _scene(11)
+    Rm = R.quat_rot(sc["rotations"])
+    M = sc["scales"][:, :, None] * Rm
+    S = M.transpose(1, 2) @ M
+    c6 = torch.stack([S[:, 0, 0], S[:, 0, 1], S[:, 0, 2], S[:, 1, 1], S[:, 1, 2], S[:, 2, 2]], 1)
+    n3 = torch.nn.functional.normalize(torch.randn(c6.shape[0], 3, dtype=torch.float64), dim=1)
+    c6d, n3d = c6.to(dev, torch.float32).requires_grad_(True), n3.to(dev, torch.float32).requires_grad_(True)
+    out, ins, _ = _ours(dm, sc, dev, cov3D=c6d, norm3D=n3d)
+    c6r, n3r = c6.clone().requires_grad_(True), n3.clone().requires_grad_(True)
+    ref, rins, _ = _reference(sc, cov3D=c6r, norm3D=n3r)
+    for k in range(4):
+        assert _close(out[k], ref[k], 1e-4) < 5e-4
+    w = _weights(sc["H"], sc["W"], seed=9)
+    _loss(out, {k: v.to(dev, torch.float32) for k, v in w.items()}).backward()
+    _loss(ref, w).backward()
+    assert _rel(c6d.grad, c6r.grad) < 2e-3 and _rel(n3d.grad, n3r.grad) < 2e-3
+    assert _rel(ins["means3D"].grad, rins["means3D"].grad) < 2e-3
+
+
+def test_module_surface_and_empty_scenes(dm):
+    import diff_gauss as dg
+    dev = torch.device("cuda")
+    sc = _scene(2, P=20)
+    st = dg.GaussianRasterizationSettings(sc["H"], sc["W"], sc["tanx"], sc["tany"], sc["bg"].to(dev, torch.float32),
+                                          1.0, sc["view"].to(dev, torch.float32), sc["proj"].to(dev, torch.float32),
+                                          0, sc["campos"].to(dev, torch.float32), False, False)
+    r = dg.GaussianRasterizer(st)
+    f = lambda k: sc[k].to(dev, torch.float32)  # noqa: E731
+    color, depth, nrm, alpha, radii, extra = r(f("means3D"), torch.zeros_like(f("means3D")), f("opacities"),
+                                               colors_precomp=f("colors"), scales=f("scales"),
+                                               rotations=f("rotations"))
+    assert color.shape == (3, sc["H"], sc["W"]) and alpha.shape == (1, sc["H"], sc["W"]) and radii.shape == (20,)
+    assert r.markVisible(f("means3D")).all()
+    with pytest.raises(Exception):
+        r(f("means3D"), torch.zeros_like(f("means3D")), f("opacities"), scales=f("scales"), rotations=f("rotations"))
+    # every Gaussian behind the camera: background only
+    behind = f("means3D").clone()
+    behind[:, 2] -= 10.0
+    color, depth, nrm, alpha, radii, _ = r(behind, torch.zeros_like(behind), f("opacities"),
+                                           colors_precomp=f("colors"), scales=f("scales"), rotations=f("rotations"))
+    assert (radii == 0).all() and float(alpha.abs().max()) == 0.0
+    assert torch.allclose(color, st.bg.view(3, 1, 1).expand_as(color))
+    # no Gaussians at all
+    z = torch.zeros((0, 3), device=dev)
+    color, *_ = r(z, z, torch.zeros((0, 1), device=dev), colors_precomp=z, scales=z,
+                  rotations=torch.zeros((0, 4), device=dev))
+    assert torch.allclose(color, st.bg.view(3, 1, 1).expand_as(color))
