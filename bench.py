@@ -399,6 +399,63 @@ def run_morph(args, device):
     }
 
 
+def run_render(args, device):
+    """The Gaussian rasterizer (diff_gauss) on the particles of the
+    configuration-5 sphere: 500k Gaussians (covariance from F = I and half a
+    grid spacing), 1024 x 1024, colors precomputed, normals from scale and
+    rotation; one step = forward + backward of an image loss.  CUDA events on
+    the current stream; the backward includes the host read of the number of
+    rendered (tile, Gaussian) pairs that sizes the sort."""
+    import torch
+    import diff_gauss as dg
+    from diffmpm_bindings import workloads as W
+    w = W.morph500k(n=50_000 if args.quick else 500_000, episode=0)
+    H = Wd = 256 if args.quick else 1024
+    tanx, tany, view, proj, eye = W.camera(H, Wd, fovx_deg=45.0, eye=(0.5, 0.5, -0.9), target=(0.5, 0.5, 0.5))
+    n = w.n
+    g = torch.Generator(device="cpu").manual_seed(0)
+    f32 = dict(dtype=torch.float32, device=device)
+    means = torch.tensor(w.x, **f32).requires_grad_(True)
+    scales = torch.full((n, 3), 0.5 * w.dx, **f32).requires_grad_(True)
+    rots = torch.nn.functional.normalize(torch.randn(n, 4, generator=g), dim=1).to(**f32).requires_grad_(True)
+    cols = torch.rand(n, 3, generator=g).to(**f32).requires_grad_(True)
+    ops = (0.3 + 0.6 * torch.rand(n, 1, generator=g)).to(**f32).requires_grad_(True)
+    st = dg.GaussianRasterizationSettings(H, Wd, tanx, tany, torch.ones(3, **f32), 1.0, view.to(**f32),
+                                          proj.to(**f32), 0, eye.to(**f32), False, False)
+    rast = dg.GaussianRasterizer(st)
+    target = torch.rand((3, H, Wd), generator=g).to(**f32)
+
+    def step():
+        m2 = torch.zeros_like(means, requires_grad=True)
+        color, depth, nrm, alpha, radii, _ = rast(means, m2, ops, colors_precomp=cols, scales=scales,
+                                                  rotations=rots)
+        loss = ((color - target) ** 2).mean() + 0.01 * alpha.mean()
+        loss.backward()
+        return radii
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(device)
+    stream = torch.cuda.current_stream(device)
+    times = []
+    with Clocks(device.index if device.index is not None else 0) as clk:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            radii = step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    return {"metric": "Gaussian rasterizer forward+backward, Gaussians/s", "value": round(n / (ms / 1e3), 1),
+            "unit": "Gaussians/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "render500k" if not args.quick else "render50k", "gaussians": n,
+                       "image": [H, Wd], "visible": int((radii > 0).sum()), "sh": "precomputed colors",
+                       "covariance": "scale 0.5 dx, random rotation", "outputs": "color, depth, normal, alpha"},
+            "clocks": clk.summary()}
+
+
 def run_e2e(torch, dm, args, w, device, keep):
     """Public API with pinned host buffers: x0, v0, F0 in; dL/dx_T seed in
     (computed on the host from x_T out, like run.py's gradient injection);
@@ -561,7 +618,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="spheres2m",
-                    choices=["spheres2m", "ellipsoid64", "sphere32", "batched", "morph500k"])
+                    choices=["spheres2m", "ellipsoid64", "sphere32", "batched", "morph500k", "render500k"])
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-particles", type=int, default=0, help="0: every particle")
     ap.add_argument("--cpu-timesteps", type=int, default=2)
@@ -600,6 +657,10 @@ def main():
     if args.workload == "morph500k":
         if rank == 0:
             print(json.dumps(run_morph(args, device)), flush=True)
+        return
+    if args.workload == "render500k":
+        if rank == 0:
+            print(json.dumps(run_render(args, device)), flush=True)
         return
     line = run_ours(args, rank, world, device)
     if rank == 0:

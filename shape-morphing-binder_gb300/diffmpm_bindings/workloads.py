@@ -254,3 +254,31 @@ def morph500k(seed=4, n=500_000, G=96, episode=0, amp=0.04, rho=None, sort=True)
     v = np.zeros_like(x)
     return Workload(f"morph500k_ep{episode}", x, v, F, m, vol, lam, mu, (G + 1,) * 3, dx, (0.0, 0.0, 0.0), dt,
                     200, rho=rho, target=tgt, extra=dict(E=E, nu=nu, ppc=ppc))
+
+
+def camera(H, W, fovx_deg=50.0, eye=(0.0, 0.0, -3.0), target=(0.0, 0.0, 0.0), znear=0.01, zfar=100.0):
+    """A look-at pinhole camera for the Gaussian rasterizer: (tanfovx, tanfovy,
+    view, proj, position) with view and proj as flat 16-vectors in the
+    rasterizer's convention (x' = m[0]x + m[4]y + m[8]z + m[12]), proj the
+    full world-to-clip transform."""
+    import torch
+    tanx = math.tan(math.radians(fovx_deg) / 2)
+    tany = tanx * H / W
+    eye_t, tgt = torch.tensor(eye, dtype=torch.float64), torch.tensor(target, dtype=torch.float64)
+    fwd = tgt - eye_t
+    fwd = fwd / fwd.norm()
+    up = torch.tensor([0.0, 1.0, 0.0], dtype=torch.float64)
+    right = torch.cross(up, fwd, dim=0)
+    right = right / right.norm()
+    up2 = torch.cross(fwd, right, dim=0)
+    Rw = torch.stack([right, up2, fwd])            # rows: camera axes in world
+    tw = -Rw @ eye_t
+    Wv = torch.eye(4, dtype=torch.float64)
+    Wv[:3, :3], Wv[:3, 3] = Rw, tw                  # column-vector world->view
+    Pr = torch.zeros(4, 4, dtype=torch.float64)
+    Pr[0, 0], Pr[1, 1] = 1 / tanx, 1 / tany
+    Pr[2, 2], Pr[2, 3] = zfar / (zfar - znear), -zfar * znear / (zfar - znear)
+    Pr[3, 2] = 1.0
+    view = Wv.T.contiguous().reshape(-1)            # flat layout m[4c+r] = Wv[r][c]
+    proj = (Pr @ Wv).T.contiguous().reshape(-1)
+    return tanx, tany, view, proj, eye_t

@@ -153,26 +153,4 @@ def render(means3D, opacities, H, W, tanfovx, tanfovy, bg, view, proj, campos, *
     return color, D.reshape(1, H, W), N.reshape(3, H, W), (1 - T).reshape(1, H, W), radii, E.reshape(ED, H, W)
 
 
-def camera(H, W, fovx_deg=50.0, eye=(0.0, 0.0, -3.0), target=(0.0, 0.0, 0.0), znear=0.01, zfar=100.0):
-    """World-to-view and full projection matrices in the rasterizer's flat
-    convention (x' = m[0]x + m[4]y + m[8]z + m[12]): a look-at camera."""
-    tanx = math.tan(math.radians(fovx_deg) / 2)
-    tany = tanx * H / W
-    eye_t, tgt = torch.tensor(eye, dtype=torch.float64), torch.tensor(target, dtype=torch.float64)
-    fwd = tgt - eye_t
-    fwd = fwd / fwd.norm()
-    up = torch.tensor([0.0, 1.0, 0.0], dtype=torch.float64)
-    right = torch.cross(up, fwd, dim=0)
-    right = right / right.norm()
-    up2 = torch.cross(fwd, right, dim=0)
-    Rw = torch.stack([right, up2, fwd])            # rows: camera axes in world
-    tw = -Rw @ eye_t
-    Wv = torch.eye(4, dtype=torch.float64)
-    Wv[:3, :3], Wv[:3, 3] = Rw, tw                  # column-vector world->view
-    Pr = torch.zeros(4, 4, dtype=torch.float64)
-    Pr[0, 0], Pr[1, 1] = 1 / tanx, 1 / tany
-    Pr[2, 2], Pr[2, 3] = zfar / (zfar - znear), -zfar * znear / (zfar - znear)
-    Pr[3, 2] = 1.0
-    view = Wv.T.contiguous().reshape(-1)            # flat layout m[4c+r] = Wv[r][c]
-    proj = (Pr @ Wv).T.contiguous().reshape(-1)
-    return tanx, tany, view, proj, eye_t
+from diffmpm_bindings.workloads import camera  # noqa: E402,F401  (re-exported for the tests)
