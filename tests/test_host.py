@@ -80,3 +80,16 @@ def test_bindings_reject_bad_render_grad_shapes(dm):
         dm.CompGraph._render_arrays(np.zeros((4, 3)), np.zeros((4, 3)), "")
     with pytest.raises(RuntimeError, match=r"dLdx must be \(N,3\)"):
         dm.CompGraph._render_arrays(np.zeros((4, 3, 3)), np.zeros((4, 2)), "")
+
+
+def test_diff_gauss_module_surface():
+    """The rasterizer module keeps the reference diff_gauss API (no GPU needed)."""
+    pytest.importorskip("torch")
+    import diff_gauss as dg
+    assert dg.GaussianRasterizationSettings._fields == (
+        "image_height", "image_width", "tanfovx", "tanfovy", "bg", "scale_modifier", "viewmatrix", "projmatrix",
+        "sh_degree", "campos", "prefiltered", "debug")
+    import inspect
+    params = list(inspect.signature(dg.GaussianRasterizer.forward).parameters)
+    assert params == ["self", "means3D", "means2D", "opacities", "shs", "colors_precomp", "scales", "rotations",
+                      "cov3Ds_precomp", "norm3Ds_precomp", "extra_attrs"]
