@@ -415,8 +415,10 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 // adjoint of k_gs_render: per pixel, walk the tile list back to front,
-// recovering T by division; the per-Gaussian terms are summed over the warp
-template <int EDMAX>
+// recovering T by division; the per-Gaussian terms are summed over the warp.
+// HD / HN: the depth / normal images have a gradient (otherwise their terms
+// vanish and are not formed)
+template <int EDMAX, bool HD, bool HN>
 __global__ void __launch_bounds__(kBlock) k_gs_render_bwd(Frame f, GsScene s, GsGeom g, const uint32_t* ids,
                                                           const uint32_t* ranges, GsImage img, const float* dLc,
                                                           const float* dLd, const float* dLn, const float* dLa,
@@ -457,8 +459,17 @@ __global__ void __launch_bounds__(kBlock) k_gs_render_bwd(Frame f, GsScene s, Gs
 #pragma unroll
     for (int e = 0; e < (EDMAX > 0 ? EDMAX : 1); ++e) acc_e[e] = prev_e[e] = 0.f;
     const float hx = 0.5f * f.W, hy = 0.5f * f.H;
-    // walk [0, n) backwards in batches; position k (0-based) is contributor k+1
-    for (int top = n; top > 0; top -= kBlock) {
+    // no pixel of the tile blends anything past the largest last contributor:
+    // start the walk there instead of at the end of the tile list
+    __shared__ int s_top;
+    if (tr == 0) s_top = 0;
+    __syncthreads();
+    const int wmax = __reduce_max_sync(0xffffffffu, last);
+    if (lane == 0) atomicMax(&s_top, wmax);
+    __syncthreads();
+    const int ntop = min(s_top, n);
+    // walk [0, ntop) backwards in batches; position k (0-based) is contributor k+1
+    for (int top = ntop; top > 0; top -= kBlock) {
         __syncthreads();
         const int cnt = min(kBlock, top);
         if (tr < cnt) {
@@ -497,19 +508,25 @@ __global__ void __launch_bounds__(kBlock) k_gs_render_bwd(Frame f, GsScene s, Gs
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch) {
                     acc_c[ch] = prev_a * prev_c[ch] + (1.f - prev_a) * acc_c[ch];
-                    acc_n[ch] = prev_a * prev_n[ch] + (1.f - prev_a) * acc_n[ch];
-                    const float c = g.rgb[3 * id + ch], nn = g.normal[3 * id + ch];
+                    const float c = g.rgb[3 * id + ch];
                     prev_c[ch] = c;
-                    prev_n[ch] = nn;
-                    dLdalpha += (c - acc_c[ch]) * gc[ch] + (nn - acc_n[ch]) * gn[ch];
+                    dLdalpha += (c - acc_c[ch]) * gc[ch];
                     o_c[ch] = w * gc[ch];
-                    o_n[ch] = w * gn[ch];
+                    if (HN) {
+                        acc_n[ch] = prev_a * prev_n[ch] + (1.f - prev_a) * acc_n[ch];
+                        const float nn = g.normal[3 * id + ch];
+                        prev_n[ch] = nn;
+                        dLdalpha += (nn - acc_n[ch]) * gn[ch];
+                        o_n[ch] = w * gn[ch];
+                    }
                 }
-                acc_d = prev_a * prev_d + (1.f - prev_a) * acc_d;
-                const float dd = g.depth[id];
-                prev_d = dd;
-                dLdalpha += (dd - acc_d) * gd;
-                o_d = w * gd;
+                if (HD) {
+                    acc_d = prev_a * prev_d + (1.f - prev_a) * acc_d;
+                    const float dd = g.depth[id];
+                    prev_d = dd;
+                    dLdalpha += (dd - acc_d) * gd;
+                    o_d = w * gd;
+                }
 #pragma unroll
                 for (int e = 0; e < EDMAX; ++e)
                     if (e < f.ED) {
@@ -535,8 +552,10 @@ __global__ void __launch_bounds__(kBlock) k_gs_render_bwd(Frame f, GsScene s, Gs
             }
             if (__any_sync(0xffffffffu, act)) {  // the whole warp works on Gaussian id
                 const float r_c0 = warp_sum(o_c[0]), r_c1 = warp_sum(o_c[1]), r_c2 = warp_sum(o_c[2]);
-                const float r_n0 = warp_sum(o_n[0]), r_n1 = warp_sum(o_n[1]), r_n2 = warp_sum(o_n[2]);
-                const float r_d = warp_sum(o_d), r_o = warp_sum(o_o), r_x = warp_sum(o_x), r_y = warp_sum(o_y);
+                const float r_n0 = HN ? warp_sum(o_n[0]) : 0.f, r_n1 = HN ? warp_sum(o_n[1]) : 0.f,
+                            r_n2 = HN ? warp_sum(o_n[2]) : 0.f;
+                const float r_d = HD ? warp_sum(o_d) : 0.f, r_o = warp_sum(o_o), r_x = warp_sum(o_x),
+                            r_y = warp_sum(o_y);
                 const float r_a = warp_sum(o_a), r_b = warp_sum(o_b), r_cc = warp_sum(o_cc);
                 float r_e[EDMAX > 0 ? EDMAX : 1];
 #pragma unroll
@@ -545,10 +564,12 @@ __global__ void __launch_bounds__(kBlock) k_gs_render_bwd(Frame f, GsScene s, Gs
                     atomicAdd(&gr.colors[3 * id], r_c0);
                     atomicAdd(&gr.colors[3 * id + 1], r_c1);
                     atomicAdd(&gr.colors[3 * id + 2], r_c2);
-                    atomicAdd(&gr.norm3D[3 * id], r_n0);
-                    atomicAdd(&gr.norm3D[3 * id + 1], r_n1);
-                    atomicAdd(&gr.norm3D[3 * id + 2], r_n2);
-                    atomicAdd(&gr.depth[id], r_d);
+                    if (HN) {
+                        atomicAdd(&gr.norm3D[3 * id], r_n0);
+                        atomicAdd(&gr.norm3D[3 * id + 1], r_n1);
+                        atomicAdd(&gr.norm3D[3 * id + 2], r_n2);
+                    }
+                    if (HD) atomicAdd(&gr.depth[id], r_d);
                     atomicAdd(&gr.opacities[id], r_o);
                     atomicAdd(&gr.means2D[3 * id], r_x);
                     atomicAdd(&gr.means2D[3 * id + 1], r_y);
@@ -828,9 +849,24 @@ extern "C" int gs_backward(const GsScene* s, const GsGeom* g, int L, const GsBin
     if (s->P == 0) return MPM_OK;
     const dim3 grid(f.gx, f.gy), block(kT, kT);
     with_ed(f.ED, [&](auto ed) {
-        k_gs_render_bwd<decltype(ed)::value><<<grid, block, 0, st>>>(f, *s, *g, b->ids_sorted, b->ranges, *img,
-                                                                      dL_dcolor, dL_ddepth, dL_dnormal, dL_dalpha,
-                                                                      dL_dextra, *out);
+        constexpr int E = decltype(ed)::value;
+        const bool hd = dL_ddepth != nullptr, hn = dL_dnormal != nullptr;
+        if (hd && hn)
+            k_gs_render_bwd<E, true, true><<<grid, block, 0, st>>>(f, *s, *g, b->ids_sorted, b->ranges, *img,
+                                                                   dL_dcolor, dL_ddepth, dL_dnormal, dL_dalpha,
+                                                                   dL_dextra, *out);
+        else if (hd)
+            k_gs_render_bwd<E, true, false><<<grid, block, 0, st>>>(f, *s, *g, b->ids_sorted, b->ranges, *img,
+                                                                    dL_dcolor, dL_ddepth, dL_dnormal, dL_dalpha,
+                                                                    dL_dextra, *out);
+        else if (hn)
+            k_gs_render_bwd<E, false, true><<<grid, block, 0, st>>>(f, *s, *g, b->ids_sorted, b->ranges, *img,
+                                                                    dL_dcolor, dL_ddepth, dL_dnormal, dL_dalpha,
+                                                                    dL_dextra, *out);
+        else
+            k_gs_render_bwd<E, false, false><<<grid, block, 0, st>>>(f, *s, *g, b->ids_sorted, b->ranges, *img,
+                                                                     dL_dcolor, dL_ddepth, dL_dnormal, dL_dalpha,
+                                                                     dL_dextra, *out);
     });
     ++g_launches;
     k_gs_preprocess_bwd<<<(s->P + 255) / 256, 256, 0, st>>>(f, *s, *g, *out);

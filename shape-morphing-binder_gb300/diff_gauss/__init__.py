@@ -142,6 +142,7 @@ class _RasterizeGaussians(torch.autograd.Function):
         im = _Image(**{k: _ptr(v) for k, v in img.items()})
         _lib.check(_lib.lib.gs_render(C.byref(sc), C.byref(g), L, C.byref(b), _vp(sort_tmp.data_ptr()),
                                       sort_b.value, C.byref(im), _stream()), "rasterize_gaussians")
+        ctx.set_materialize_grads(False)  # unused outputs arrive as None: their adjoint terms are skipped
         ctx.raster_settings = s
         ctx.num_rendered = L
         ctx.has = dict(sh=sh.numel() > 0, colors=colors_precomp.numel() > 0, scales=scales.numel() > 0,
