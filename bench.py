@@ -260,7 +260,7 @@ def run_ours(args, rank, world, device):
         if cnt.value:
             kern[lib.mpm_kernel_name(k).decode()] = (cnt.value, ms.value)
     t_total = max_over_ranks(torch, sum(times), world, device)
-    value = world * n * T * args.steps / t_total
+    value = job_value(world, n * T * args.steps, t_total)
     active = cg.active_nodes(0)
 
     # ---- roofline of the dominant kernel
@@ -600,6 +600,12 @@ def barrier(world):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
+
+
+def job_value(world, units_per_rank, t_max):
+    """Whole-job throughput of independent replicas (weak scaling): every rank
+    processes the same units; the job takes the slowest rank's time."""
+    return world * units_per_rank / t_max
 
 
 def max_over_ranks(torch, t, world, device):
