@@ -50,7 +50,7 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def make_workload(name: str, quick: bool = False, timesteps: int = 0):
+def make_workload(name: str, quick: bool = False, timesteps: int = 0, checkpoint: int = 0):
     from diffmpm_bindings import workloads as W
     if name == "spheres2m":
         w = W.spheres2m(n=200_000 if quick else 2_000_000, steps=40 if quick else 400, checkpoint=20)
@@ -65,6 +65,8 @@ def make_workload(name: str, quick: bool = False, timesteps: int = 0):
         raise SystemExit(f"unknown workload {name}")
     if timesteps:
         w.steps = timesteps
+    if checkpoint:
+        w.checkpoint = checkpoint
     if w.target is None:
         rng = np.random.default_rng(11)
         w.target = w.x + 0.02 * np.sin(2 * np.pi * w.x[:, [1, 2, 0]] + rng.random(3))
@@ -212,7 +214,7 @@ def run_ours(args, rank, world, device):
         w.target = tgt_np
         args.no_e2e, args.no_fp64, args.no_cpu = True, True, True
     else:
-        w = make_workload(args.workload, args.quick, args.timesteps)
+        w = make_workload(args.workload, args.quick, args.timesteps, args.checkpoint)
         if args.shuffle:
             p = np.random.default_rng(5).permutation(w.n)
             for k in ("x", "v", "F", "m", "vol", "lam", "mu", "target"):
@@ -632,6 +634,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="reduced workload for smoke runs")
     ap.add_argument("--timesteps", type=int, default=0, help="override the workload's timestep count")
+    ap.add_argument("--checkpoint", type=int, default=0,
+                    help="override the workload's checkpoint interval (1: full tape, no recomputation)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--deterministic", action="store_true",
