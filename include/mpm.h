@@ -232,6 +232,11 @@ int mpm_compgraph_loss_history(const mpm_compgraph* cg, double* out, int cap, in
 void mpm_step_count(long long* forward_steps, long long* backward_steps);
 /* number of grid nodes with mass > 0 in the forward grid of `layer` */
 int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long* out);
+/* No counterpart in the reference (which only tests the loss with
+ * std::isfinite, CompGraph.cpp:290-293): *flag = 1 if the state planes of
+ * `layer` (x, v, C, F; with grads != 0 also its gradient planes) hold a NaN
+ * or Inf, else 0.  One pass over the planes; the layer must be stored. */
+int mpm_compgraph_nonfinite(mpm_compgraph* cg, int layer, int grads, int* flag);
 /* number of grid nodes with mass > 0 in the forward grid of `layer` (the
  * last forward step's grid when the graph is checkpointed) -- see above */
 

@@ -2009,6 +2009,30 @@ int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long*
     });
 }
 
+int mpm_compgraph_nonfinite(mpm_compgraph* cg, int layer, int grads, int* flag)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (!flag) fail(MPM_ERR_ARG, "null output");
+        if (layer < 0 || layer >= (int)G.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
+        const std::shared_ptr<PCData>& d = G.layers[layer].pc;
+        if (!d || !d->have_state) fail(MPM_ERR_STATE, "layer %d is not stored", layer);
+        DevBuf f(sizeof(int));
+        ck(cudaMemsetAsync(f.p, 0, sizeof(int), G.stream), "memset");
+        with_prec(G.prec, [&](auto r) {
+            using R = decltype(r);
+            launch_nonfinite<R>(d->n, ST_N, d->ld, d->st->as<R>(), f.as<int>(), G.stream);
+            if (grads && d->grads) launch_nonfinite<R>(d->n, ST_N, d->ld, d->grads->as<R>(), f.as<int>(), G.stream);
+        });
+        check_launch("nonfinite");
+        int h = 0;
+        ck(cudaMemcpyAsync(&h, f.p, sizeof h, cudaMemcpyDeviceToHost, G.stream), "D2H");
+        ck(cudaStreamSynchronize(G.stream), "sync");
+        *flag = h != 0;
+    });
+}
+
 int mpm_profile_enable(int on)
 {
     return guard([&] {

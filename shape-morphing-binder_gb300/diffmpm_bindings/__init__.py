@@ -564,6 +564,12 @@ class CompGraph:
         check(lib.mpm_compgraph_adam_step(self._h, int(layer), float(alpha), float(grad_norm), float(beta1),
                                           float(beta2), float(eps), int(timestep)))
 
+    def has_nonfinite(self, layer: int, grads: bool = False) -> bool:
+        """NaN/Inf anywhere in the layer's state (and gradient) planes (additive)."""
+        f = C.c_int()
+        check(lib.mpm_compgraph_nonfinite(self._h, int(layer), int(bool(grads)), C.byref(f)))
+        return bool(f.value)
+
     def active_nodes(self, layer: int = 0) -> int:
         out = C.c_ulonglong()
         check(lib.mpm_compgraph_active_nodes(self._h, int(layer), C.byref(out)))

@@ -100,6 +100,7 @@ _SIGS = {
     "mpm_compgraph_set_tuning": [_vp, C.c_int, C.c_int],
     "mpm_compgraph_set_deterministic": [_vp, C.c_int],
     "mpm_compgraph_resort": [_vp],
+    "mpm_compgraph_nonfinite": [_vp, C.c_int, C.c_int, _ip],
     "mpm_winding_numbers": [C.c_int, _vp, C.c_int, _vp, _vp, C.c_int, _vp],
     # Gaussian-splatting rasterizer (include/gsplat.h; structs passed by pointer)
     "gs_scratch_bytes": [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)],

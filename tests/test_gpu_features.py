@@ -356,3 +356,23 @@ def test_autotune_picks_a_valid_configuration(dm, orc):
     cg.compute_forward_pass(0, 0)
     want, _ = orc.forward_step(g, prm, s0)
     assert rel_err(cg.get_point_cloud(1).get("x", np.float64), want.x) < 1e-6
+
+
+def test_nonfinite_state_is_flagged_not_fatal(dm):
+    """A NaN injected on the host flows through a pass without faulting and is
+    reported by the state check; a clean state is not flagged."""
+    s0, g, rng, _, _ = _case(14, G=10)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
+    T = 3
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=T + 1)
+    cg.compute_forward_pass(0, 0)
+    assert not cg.has_nonfinite(T)
+    v = s0.v.copy()
+    v[7, 1] = np.nan
+    cg.get_point_cloud(0).set("v", v)
+    cg.compute_forward_pass(0, 0)
+    assert cg.has_nonfinite(T) and cg.has_nonfinite(0)
+    v[7, 1] = 0.0
+    cg.get_point_cloud(0).set("v", v)
+    cg.compute_forward_pass(0, 0)
+    assert not cg.has_nonfinite(T)
