@@ -815,7 +815,8 @@ void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& 
     }
     check_launch("grid_adj");
     R* gctl = nullptr;
-    if (c.exact) gctl = ensure(a.gctl, a.planes_bytes(9), s, false)->as<R>();
+    // zeroed once: the padding rows between batched instances are never written
+    if (c.exact) gctl = ensure(a.gctl, a.planes_bytes(9), s, true)->as<R>();
     R *glam = nullptr, *gmu = nullptr;
     if (G.lame_on && G.glame) {
         glam = G.glame->as<R>();

@@ -96,3 +96,23 @@ def test_batch_rejects_mass_loss(dm):
     cg = dm.CompGraph.batch(pcs, grids)
     with pytest.raises(RuntimeError, match="single-instance"):
         cg.end_layer_mass_loss()
+
+
+def test_batch_padding_rows_stay_zero(dm):
+    """The rows between instances (each instance starts at a multiple of 256)
+    are no particles: their gradients read back as zero, however the device
+    memory behind them was used before."""
+    insts = _instances(seed=4, count=3)
+    pcs = [_pc(dm, s, "fp32") for s, g, _ in insts]
+    grids = [dm.Grid(*g.dims, g.dx, g.min) for s, g, _ in insts]
+    for det in (False, True):
+        cg = dm.CompGraph.batch(pcs, grids, adjoint="exact", deterministic=det)
+        n_total = len(cg.get_point_cloud(0))
+        ranges = [cg.instance_range(i) for i in range(len(insts))]
+        _, g0 = _run(cg, 4, [sd for _, _, sd in insts], ranges, n_total)
+        pad = np.ones(n_total, bool)
+        for r in ranges:
+            pad[r] = False
+        assert pad.any()
+        for k, g in g0.items():
+            assert not np.any(g[pad]), k
