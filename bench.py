@@ -54,6 +54,7 @@ def make_workload(name: str, quick: bool = False, timesteps: int = 0, checkpoint
     from diffmpm_bindings import workloads as W
     if name == "spheres2m":
         w = W.spheres2m(n=200_000 if quick else 2_000_000, steps=40 if quick else 400, checkpoint=20)
+        w.extra["grad_E"] = True  # gradients w.r.t. control F, v0 and the scalar E
     elif name == "ellipsoid64":
         w = W.ellipsoid64(steps=20 if quick else 100, checkpoint=10)
     elif name == "sphere32":
@@ -223,6 +224,8 @@ def run_ours(args, rank, world, device):
         cg, keep = build_graph(dm, w, "fp32", w.checkpoint, deterministic=args.deterministic)
         n_pad = n
     cg.set_resort(not args.no_resort)
+    if w.extra.get("grad_E"):
+        cg.enable_lame_grads(True)
     cg.set_up_comp_graph(T + 1)
     stream = torch.cuda.current_stream(device)
     cg.set_stream(stream)
@@ -312,7 +315,9 @@ def run_ours(args, rank, world, device):
                    "bench_step": "one rollout: forward T steps + loss gradient + backward T steps",
                    "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic),
                    "particle_order": ("shuffled" if args.shuffle else "cell-sorted input") +
-                                     ("" if args.no_resort else ", re-sorted by cell at set-up")},
+                                     ("" if args.no_resort else ", re-sorted by cell at set-up"),
+                   "gradients": "layer 0: x, v, F, C, control F" + (", lam, mu (dL/dE)" if w.extra.get("grad_E")
+                                                                    else "")},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
         "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
     }
@@ -468,6 +473,9 @@ def run_e2e(torch, dm, args, w, device, keep):
                       deterministic=args.deterministic, kernel=w.extra.get("kernel", "cubic"),
                       material=w.extra.get("material", "fcr"))
     cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
+    grad_E = bool(w.extra.get("grad_E"))
+    if grad_E:
+        cg.enable_lame_grads(True)
     cg.set_up_comp_graph(T + 1)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).pin_memory()  # noqa: E731
     hx, hv, hF = pin(w.x), pin(w.v), pin(w.F)
@@ -475,9 +483,14 @@ def run_e2e(torch, dm, args, w, device, keep):
     out_x = torch.empty((n, 3), dtype=torch.float32).pin_memory()
     out_gv = torch.empty((n, 3), dtype=torch.float32).pin_memory()
     out_gF = torch.empty((n, 3, 3), dtype=torch.float32).pin_memory()
+    out_gl = torch.empty((n,), dtype=torch.float32).pin_memory()
+    out_gm = torch.empty((n,), dtype=torch.float32).pin_memory()
     seed = torch.empty((n, 3), dtype=torch.float32).pin_memory()
     h2d = (hx.numel() + hv.numel() + hF.numel() + seed.numel()) * 4
-    d2h = (out_x.numel() + out_gv.numel() + out_gF.numel()) * 4
+    d2h = (out_x.numel() + out_gv.numel() + out_gF.numel() + (2 * n if grad_E else 0)) * 4
+    if grad_E:
+        nu = float(w.extra["nu"])
+        dlam, dmu = nu / ((1 + nu) * (1 - 2 * nu)), 1.0 / (2 * (1 + nu))  # d(lam, mu)/dE
     import ctypes as C
     lib = dm._lib.lib
 
@@ -496,7 +509,12 @@ def run_e2e(torch, dm, args, w, device, keep):
         last.set("grad_x", seed.numpy())
         cg.compute_backward_pass(0)
         get_into(l0, "grad_v", out_gv)
-        get_into(l0, "grad_F", out_gF)
+        get_into(l0, "grad_dFc", out_gF)
+        if grad_E:
+            get_into(l0, "grad_lam", out_gl)
+            get_into(l0, "grad_mu", out_gm)
+            return float(out_gl.numpy().sum(dtype=np.float64) * dlam + out_gm.numpy().sum(dtype=np.float64) * dmu)
+        return None
 
     for _ in range(max(1, min(args.warmup, 2))):
         step()
@@ -510,7 +528,8 @@ def run_e2e(torch, dm, args, w, device, keep):
     t = sum(ts)
     return {"value": round(n * T * k / t, 1), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": round(1e3 * t / k, 3),
-            "path": "diffmpm_bindings.CompGraph (C ABI) from pinned host buffers"}
+            "path": "diffmpm_bindings.CompGraph (C ABI) from pinned host buffers",
+            "outputs": "x_T; dL/dv0, dL/d(control F)" + (", dL/dE" if grad_E else "")}
 
 
 def run_fp64(torch, dm, w, device, args):
@@ -522,6 +541,8 @@ def run_fp64(torch, dm, w, device, args):
     grads = {}
     for prec in ("fp64", "fp32"):
         cg, keep = build_graph(dm, w, prec, w.checkpoint)
+        if w.extra.get("grad_E"):
+            cg.enable_lame_grads(True)
         cg.set_up_comp_graph(T + 1)
         tdt = torch.float64 if prec == "fp64" else torch.float32
         tgt = torch.tensor(w.target, dtype=tdt, device=device)
@@ -537,12 +558,17 @@ def run_fp64(torch, dm, w, device, args):
         res[prec] = n * T / (e0.elapsed_time(e1) / 1e3)
         grads[prec] = {"x": cg.get_point_cloud(T).get("x", np.float64),
                        "gv": cg.get_grad(0, "v", np.float64), "gF": cg.get_grad(0, "dFc", np.float64)}
+        if w.extra.get("grad_E"):
+            nu = float(w.extra["nu"])
+            grads[prec]["gE"] = np.array([cg.get_grad(0, "lam", np.float64).sum() * nu / ((1 + nu) * (1 - 2 * nu))
+                                          + cg.get_grad(0, "mu", np.float64).sum() / (2 * (1 + nu))])
         del cg, keep
     rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))  # noqa: E731
     return {"value": round(res["fp64"], 1), "unit": UNIT, "timesteps": T,
             "fp32_value_same_rollout": round(res["fp32"], 1), "speedup_fp32_vs_fp64": round(res["fp32"] / res["fp64"], 2),
             "grad_v0_rel_err": rel(grads["fp32"]["gv"], grads["fp64"]["gv"]),
             "grad_dFc_rel_err": rel(grads["fp32"]["gF"], grads["fp64"]["gF"]),
+            **({"grad_E_rel_err": rel(grads["fp32"]["gE"], grads["fp64"]["gE"])} if "gE" in grads["fp32"] else {}),
             "x_T_max_abs_err": float(np.abs(grads["fp32"]["x"] - grads["fp64"]["x"]).max())}
 
 

@@ -1232,6 +1232,9 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP
     load_planes(st + ST_C * ld, ld, p, 9, C);
     load_Ft(st, dfc, ld, p, F, Ft);
     const R mass = co[CO_M * ld + p], vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
+    // running Lame gradient sums, read here so that the read is not the
+    // last dependency of the block
+    const R glam0 = glam ? glam[p] : R(0), gmu0 = gmu ? gmu[p] : R(0);
     Inv<R> iv;
     invariants(Ft, iv);
     R P[9], Rm[9], S[9], PF[9], A[9];
@@ -1421,8 +1424,8 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP
                 dl += gP[i] * lj * iv.Fit[i];
             }
         }
-        if (gmu) gmu[p] += dm;
-        if (glam) glam[p] += dl;
+        if (gmu) gmu[p] = gmu0 + dm;
+        if (glam) glam[p] = glam0 + dl;
     }
 }
 
