@@ -273,6 +273,8 @@ def run_ours(args, rank, world, device):
     top = max((k for k in kern if k in KERNEL_BYTES), key=lambda k: kern[k][1])
     cnt, ms = kern[top]
     bp, bn = KERNEL_BYTES[top]
+    if top == "p2g_adj" and w.extra.get("grad_E"):
+        bp += 16  # read and write the running dL/dlam, dL/dmu
     algo = bp * n + bn * active
     achieved = algo / (ms / cnt / 1e3) / 1e9
     traffic = None
