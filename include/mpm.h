@@ -257,10 +257,19 @@ long long mpm_launch_count(void);
  * see mpm_set_scatter_mode / mpm_set_tile_nodes) */
 int mpm_compgraph_set_tuning(mpm_compgraph* cg, int tile_nodes, int scatter_mode);
 int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scatter_mode);
+/* node-tile budgets of the adjoint kernels (FP32): the G2P transpose's
+ * scatter and the P2G transpose's gather, whose best sizes differ from P2G's
+ * (-1: follow the set_tuning budget, the default; 0..2816 nodes); get
+ * returns the budgets in effect */
+int mpm_compgraph_set_adjoint_tiles(mpm_compgraph* cg, int scatter_nodes, int gather_nodes);
+int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes, int* gather_nodes);
 /* No counterpart in the reference: time `steps`-step forward+backward passes
  * of a scratch copy of this graph (layer 0's state) for each candidate
- * scatter strategy and tile budget, keep the fastest for this graph and
- * return it (best_ms: one timed forward+backward of the candidate) */
+ * scatter strategy and P2G tile budget, then for each budget of the G2P
+ * transpose's scatter tile and of the P2G transpose's gather tile (one at a
+ * time, the others held), keep the fastest for this graph and return P2G's
+ * choice (best_ms: one timed forward+backward of the winner; the adjoint
+ * budgets: mpm_compgraph_get_adjoint_tiles) */
 int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms);
 /* record forward/backward passes as CUDA graphs and replay them (1 = on,
  * the default): a pass is recorded the second time it runs with the same

@@ -555,6 +555,8 @@ struct Graph {
     std::map<std::string, std::unique_ptr<Cap>> caps;
     bool graphs_on = true;
     int tile_nodes = -1, scatter_mode = -1;  // tuning (-1: library defaults)
+    int adj_tile_nodes = -1;                 // G2P-transpose scatter tile (-1: tile_nodes)
+    int gather_tile_nodes = -1;              // P2G-transpose gather tile (-1: tile_nodes)
     // deterministic scatters (opt.deterministic): fixed-point node
     // accumulators, their control words and the adjoint scatter's inputs
     Buf fix, fctl, fscr;
@@ -591,6 +593,8 @@ struct Graph {
         c.exact = opt.adjoint == MPM_ADJ_EXACT;
         c.tile_nodes = tile_nodes;
         c.scatter_mode = scatter_mode;
+        c.adj_tile_nodes = adj_tile_nodes;
+        c.gather_tile_nodes = gather_tile_nodes;
         double max_dx = geom.dx;
         if (!inst.empty()) {
             c.inst = inst_table->p;
@@ -2087,6 +2091,28 @@ int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scat
     });
 }
 
+int mpm_compgraph_set_adjoint_tiles(mpm_compgraph* cg, int scatter_nodes, int gather_nodes)
+{
+    return guard([&] {
+        check_cg(cg);
+        for (int v : {scatter_nodes, gather_nodes})
+            if (v < -1 || v > 2816) fail(MPM_ERR_ARG, "adjoint tile nodes must be -1 or in [0, 2816]");
+        cg->g.adj_tile_nodes = scatter_nodes;
+        cg->g.gather_tile_nodes = gather_nodes;
+    });
+}
+
+int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes, int* gather_nodes)
+{
+    return guard([&] {
+        check_cg(cg);
+        const Graph& G = cg->g;
+        const int base = G.tile_nodes >= 0 ? G.tile_nodes : g_tile_nodes;
+        if (scatter_nodes) *scatter_nodes = G.adj_tile_nodes >= 0 ? G.adj_tile_nodes : base;
+        if (gather_nodes) *gather_nodes = G.gather_tile_nodes >= 0 ? G.gather_tile_nodes : base;
+    });
+}
+
 int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms)
 {
     return guard([&] {
@@ -2112,41 +2138,75 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
         T.layers.resize(1);
         T.layers[0].pc = T.base;
         const int tiles[] = {0, 512, 1024, 2048};
+        const int adj_tiles[] = {512, 1024, 2048};
+        const int gather_tiles[] = {1024, 2048, 2816};
         double best = 1e300;
-        int bt = -1, bm = -1;
+        int bt = -1, bm = -1, ba = -1, bg = -1;
         cudaEvent_t e0, e1;
         ck(cudaEventCreate(&e0), "event");
         ck(cudaEventCreate(&e1), "event");
         with_prec(G.prec, [&](auto r) {
             using R = decltype(r);
             graph_set_up<R>(T, steps + 1);
-            for (int mode = (G.prec == MPM_FP32 ? 1 : 0); mode >= 0; --mode)
+            // eager, recorded, then timed replay (graphs) or third eager run
+            auto time_pass = [&]() {
+                for (int rep = 0; rep < 3; ++rep) {
+                    if (rep == 2) ck(cudaEventRecord(e0, s), "event");
+                    graph_forward<R>(T, 0);
+                    graph_backward<R>(T, 0);
+                    if (rep == 2) ck(cudaEventRecord(e1, s), "event");
+                }
+                ck(cudaEventSynchronize(e1), "event");
+                float ms = 0;
+                ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+                return (double)ms;
+            };
+            // one budget at a time, the others held: 1. scatter strategy and
+            // P2G's tile; 2. the G2P transpose's tile; 3. the P2G transpose's
+            // gather tile
+            const bool fp32 = G.prec == MPM_FP32;
+            T.adj_tile_nodes = fp32 ? 1024 : -1;
+            T.gather_tile_nodes = fp32 ? 2048 : -1;
+            for (int mode = (fp32 ? 1 : 0); mode >= 0; --mode)
                 for (int tile : tiles) {
-                    if (G.prec != MPM_FP32 && tile != 0) continue;
+                    if (!fp32 && tile != 0) continue;
                     if (G.opt.deterministic && mode != 1) continue;  // the fixed-point scatter is segmented
                     T.tile_nodes = tile;
                     T.scatter_mode = mode;
-                    // eager, recorded, then timed replay (graphs) or third eager run
-                    for (int rep = 0; rep < 3; ++rep) {
-                        if (rep == 2) ck(cudaEventRecord(e0, s), "event");
-                        graph_forward<R>(T, 0);
-                        graph_backward<R>(T, 0);
-                        if (rep == 2) ck(cudaEventRecord(e1, s), "event");
-                    }
-                    ck(cudaEventSynchronize(e1), "event");
-                    float ms = 0;
-                    ck(cudaEventElapsedTime(&ms, e0, e1), "event");
+                    const double ms = time_pass();
                     if (ms < best) {
                         best = ms;
                         bt = tile;
                         bm = mode;
                     }
                 }
+            if (fp32) {
+                T.tile_nodes = bt;
+                T.scatter_mode = bm;
+                auto sweep = [&](const int* cand, int nc, int& field, int held) {
+                    int pick = held;
+                    for (int q = 0; q < nc; ++q) {
+                        if (cand[q] == held) continue;  // timed already
+                        field = cand[q];
+                        const double ms = time_pass();
+                        if (ms < best) {
+                            best = ms;
+                            pick = cand[q];
+                        }
+                    }
+                    field = pick;
+                    return pick;
+                };
+                ba = sweep(adj_tiles, 3, T.adj_tile_nodes, 1024);
+                bg = sweep(gather_tiles, 3, T.gather_tile_nodes, 2048);
+            }
         });
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         G.tile_nodes = bt;
         G.scatter_mode = bm;
+        G.adj_tile_nodes = ba;
+        G.gather_tile_nodes = bg;
         if (best_tile) *best_tile = bt;
         if (best_mode) *best_mode = bm;
         if (best_ms) *best_ms = best;

@@ -1795,6 +1795,20 @@ int tile_cap_for(const StepCfg& c)
     return sizeof(R) == 4 ? (c.tile_nodes >= 0 ? c.tile_nodes : g_tile_nodes) : 0;
 }
 
+// the G2P transpose's scatter tile and the P2G transpose's gather tile:
+// their own budgets when the graph sets them, else P2G's
+template <typename R>
+int adj_cap_for(const StepCfg& c)
+{
+    return sizeof(R) == 4 && c.adj_tile_nodes >= 0 ? c.adj_tile_nodes : tile_cap_for<R>(c);
+}
+
+template <typename R>
+int gather_cap_for(const StepCfg& c)
+{
+    return sizeof(R) == 4 && c.gather_tile_nodes >= 0 ? c.gather_tile_nodes : tile_cap_for<R>(c);
+}
+
 inline int scatter_mode_of(const StepCfg& c) { return c.scatter_mode >= 0 ? c.scatter_mode : g_scatter_mode; }
 
 }  // namespace
@@ -1929,7 +1943,7 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
                     const R* trust, R* adj, cudaStream_t s)
 {
     if (n <= 0) return;
-    const int cap = tile_cap_for<R>(c);
+    const int cap = adj_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
         if (c.det()) {
@@ -1994,7 +2008,7 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
 {
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
-    const int cap = tile_cap_for<R>(c);
+    const int cap = gather_cap_for<R>(c);
     const size_t sm = (size_t)cap * 2 * sizeof(float4);
     if (c.kernel == 0) {
         ensure_smem(k_p2g_adj<R, 4>, sm);

@@ -32,9 +32,15 @@ struct StepCfg {
     const void* inst = nullptr;
     int ninst = 0;
     long long total_nodes = 0;
-    // per-graph tuning (-1: the process-wide defaults below)
+    // per-graph tuning (-1: the process-wide defaults below).  tile_nodes is
+    // the node-tile budget of P2G's scatter; adj_tile_nodes that of the G2P
+    // transpose's scatter and gather_tile_nodes that of the P2G transpose's
+    // gather (-1: tile_nodes).  Their best sizes differ: the G2P transpose
+    // fits a fourth block per SM under 1024 nodes, the gather wants 2048+.
     int tile_nodes = -1;
     int scatter_mode = -1;
+    int adj_tile_nodes = -1;
+    int gather_tile_nodes = -1;
     // Deterministic scatters (FP32 segmented path): node sums accumulate in
     // 64-bit fixed point, so their value does not depend on the order of the
     // atomics.  fix: 4 words per node, all zero between steps (the grid

@@ -419,15 +419,23 @@ class CompGraph:
         by timing short forward+backward passes (additive)."""
         t, m, ms = C.c_int(), C.c_int(), C.c_double()
         check(lib.mpm_compgraph_autotune(self._h, int(steps), C.byref(t), C.byref(m), C.byref(ms)), "autotune")
-        return {"tile_nodes": t.value, "scatter_mode": m.value, "ms_per_pass": ms.value, "steps": int(steps)}
+        out = self.get_tuning()
+        out.update(ms_per_pass=ms.value, steps=int(steps))
+        return out
 
-    def set_tuning(self, tile_nodes=-1, scatter_mode=-1):
+    def set_tuning(self, tile_nodes=-1, scatter_mode=-1, adj_tile_nodes=-1, gather_tile_nodes=-1):
+        """P2G's tile budget and the scatter strategy, and the tile budgets of
+        the G2P transpose's scatter and the P2G transpose's gather (-1:
+        library defaults; the adjoint budgets follow P2G's)."""
         check(lib.mpm_compgraph_set_tuning(self._h, int(tile_nodes), int(scatter_mode)))
+        check(lib.mpm_compgraph_set_adjoint_tiles(self._h, int(adj_tile_nodes), int(gather_tile_nodes)))
 
     def get_tuning(self) -> dict:
-        t, m = C.c_int(), C.c_int()
+        t, m, at, gt = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(lib.mpm_compgraph_get_tuning(self._h, C.byref(t), C.byref(m)))
-        return {"tile_nodes": t.value, "scatter_mode": m.value}
+        check(lib.mpm_compgraph_get_adjoint_tiles(self._h, C.byref(at), C.byref(gt)))
+        return {"tile_nodes": t.value, "scatter_mode": m.value, "adj_tile_nodes": at.value,
+                "gather_tile_nodes": gt.value}
 
     def use_graphs(self, on=True):
         """Replay forward/backward passes as CUDA graphs (default on)."""

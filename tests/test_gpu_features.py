@@ -352,10 +352,39 @@ def test_autotune_picks_a_valid_configuration(dm, orc):
     cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=3)
     res = cg.autotune(steps=2)
     assert res["tile_nodes"] in (0, 512, 1024, 2048) and res["scatter_mode"] in (0, 1) and res["ms_per_pass"] > 0
-    assert cg.get_tuning() == {"tile_nodes": res["tile_nodes"], "scatter_mode": res["scatter_mode"]}
+    assert res["adj_tile_nodes"] in (512, 1024, 2048) and res["gather_tile_nodes"] in (1024, 2048, 2816)
+    assert cg.get_tuning() == {k: res[k] for k in ("tile_nodes", "scatter_mode", "adj_tile_nodes",
+                                                   "gather_tile_nodes")}
     cg.compute_forward_pass(0, 0)
     want, _ = orc.forward_step(g, prm, s0)
     assert rel_err(cg.get_point_cloud(1).get("x", np.float64), want.x) < 1e-6
+
+
+def test_adjoint_tile_budgets_change_no_result(dm):
+    """The adjoint kernels' own tile budgets (or tiles off): the P2G
+    transpose's gather reads the same node values from the tile as from
+    global memory, and the G2P transpose's fixed-point scatter sums the same
+    integers, so the gradients are identical."""
+    s0, g, rng, _, _ = _case(15, G=12)
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.1, exact=True)
+    T = 3
+    seed = rng.normal(size=(s0.n, 3)) / s0.n
+    outs = []
+    for at, gt in ((-1, -1), (0, 0), (512, 64), (2048, 2816)):
+        cg, keep = make_graph(dm, s0, g, prm, precision="fp32", adjoint="exact", layers=T + 1,
+                              deterministic=True)
+        cg.set_tuning(1024, 1, at, gt)
+        tun = cg.get_tuning()
+        assert (tun["adj_tile_nodes"], tun["gather_tile_nodes"]) == (1024 if at < 0 else at, 1024 if gt < 0 else gt)
+        cg.compute_forward_pass(0, 0)
+        last = cg.get_point_cloud(T)
+        last.set("grad_x", seed)
+        cg.compute_backward_pass(0)
+        outs.append({k: cg.get_grad(0, k, np.float32) for k in ("x", "v", "F", "C", "dFc")})
+    for o in outs[1:]:
+        for k in o:
+            assert np.array_equal(o[k], outs[0][k]), k
+    assert dm._lib.lib.mpm_compgraph_set_adjoint_tiles(cg._h, 5000, -1) == dm._lib.MPM_ERR_ARG
 
 
 def test_nonfinite_state_is_flagged_not_fatal(dm):
