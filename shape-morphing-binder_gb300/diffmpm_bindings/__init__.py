@@ -563,6 +563,26 @@ class CompGraph:
         """dL/d{x,v,F,C,dFc,lam,mu} of a layer after compute_backward_pass."""
         return self.get_point_cloud(layer).get("grad_" + field, dtype)
 
+    def get_grad_v0(self, dtype=np.float32) -> np.ndarray:
+        """dL/dv of layer 0, (N, 3)."""
+        return self.get_grad(0, "v", dtype)
+
+    def get_grad_F(self, layer: int = 0, dtype=np.float32) -> np.ndarray:
+        """dL/d(control F) of a layer, (N, 3, 3): the gradient the control
+        optimisation descends (ForwardSimulation.cpp uses F + dFc)."""
+        return self.get_grad(layer, "dFc", dtype)
+
+    def get_grad_E(self, young_modulus: float, layer: int = 0) -> float:
+        """dL/dE for a material whose Lame parameters all scale with one
+        Young's modulus E at fixed Poisson ratio (lam, mu proportional to E):
+        (sum dL/dlam * lam + sum dL/dmu * mu) / E.  Needs
+        enable_lame_grads(True) before the backward pass; the sums run from
+        `layer` (the control layer of that pass) to the end."""
+        pc = self.get_point_cloud(layer)
+        glam, gmu = pc.get("grad_lam", np.float64), pc.get("grad_mu", np.float64)
+        lam, mu = pc.get("lam", np.float64), pc.get("mu", np.float64)
+        return float((glam @ lam + gmu @ mu) / float(young_modulus))
+
     def grad_norm(self, layer: int) -> float:
         out = C.c_double()
         check(lib.mpm_compgraph_grad_norm(self._h, int(layer), C.byref(out)))

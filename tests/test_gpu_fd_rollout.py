@@ -131,3 +131,29 @@ def test_rollout_gradient_matches_finite_differences(twin, fd, adjoint, precisio
           f"gradient vs oracle adjoint {rel(g_fc, o_fc):.2e} (dFc) {rel(g_v, o_v):.2e} (v0) "
           f"{abs(g_E - o_E) / abs(o_E):.2e} (E)")
     assert err.max() <= tol, err
+
+
+def test_compgraph_gradient_accessors_match_oracle_adjoint(dm, twin, adjoint):
+    """get_grad_v0 / get_grad_F / get_grad_E of a CompGraph backward pass
+    (FP64, checkpoint every 20, Lame gradients on) against the oracle's FP64
+    exact adjoint of the same rollout and loss."""
+    w, tgt, dfc, _ = twin
+    n = w.n
+    E, nu = w.extra["E"], w.extra["nu"]
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 + 2 * nu)  # in double, as the oracle
+    pc = dm.PointCloud.from_arrays(w.x, v=w.v, F=w.F, dFc=dfc, m=w.m, vol=w.vol, lam=np.full(n, lam),
+                                   mu=np.full(n, mu), precision="fp64")
+    grid = dm.Grid(*w.dims, w.dx, (0.0, 0.0, 0.0), precision="fp64")
+    cg = dm.CompGraph(pc, grid, grid, adjoint="exact", checkpoint_every=20)
+    cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
+    cg.enable_lame_grads(True)
+    cg.set_up_comp_graph(T + 1)
+    cg.compute_forward_pass(0, 0)
+    last = cg.get_point_cloud(T)
+    last.set("grad_x", 2.0 * (last.get("x", np.float64) - tgt) / (3 * n))  # d mean((x_T - tgt)^2) / dx_T
+    cg.compute_backward_pass(0)
+    o_fc, o_v, o_E = adjoint
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    assert rel(cg.get_grad_F(0, np.float64), o_fc) <= 1e-10
+    assert rel(cg.get_grad_v0(np.float64), o_v) <= 1e-10
+    assert abs(cg.get_grad_E(w.extra["E"]) - o_E) <= 1e-10 * abs(o_E)
