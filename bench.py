@@ -58,7 +58,7 @@ def make_workload(name: str, quick: bool = False, timesteps: int = 0, checkpoint
     elif name == "ellipsoid64":
         w = W.ellipsoid64(steps=20 if quick else 100, checkpoint=10)
     elif name == "sphere32":
-        # configuration 1 as stated: Neo-Hookean, quadratic B-spline APIC
+        # the 17k-particle sphere as specified: Neo-Hookean, quadratic B-spline APIC
         w = W.sphere32()
         w.checkpoint = 1
         w.extra.update(kernel="quadratic", material="neohookean")
@@ -132,7 +132,7 @@ class Clocks:
 # --------------------------------------------------------------- our arm
 
 # algorithmic bytes per particle and per active node for each kernel (FP32
-# storage; see DESIGN.md "Roofline accounting")
+# storage)
 KERNEL_BYTES = {
     "p2g": (112, 16),
     "g2p": (148, 16),
@@ -168,7 +168,7 @@ def device_rollout(torch, cg, T, tgt, n):
 
 
 class BatchWorkload:
-    """BASELINE configuration 3 as one workload: 64 instances concatenated."""
+    """The batched workload: 64 instances of uneven size concatenated."""
 
     def __init__(self, quick=False, timesteps=0):
         from diffmpm_bindings import workloads as W
@@ -331,7 +331,7 @@ def run_ours(args, rank, world, device):
 
 
 def run_morph(args, device):
-    """BASELINE configuration 5 end to end: a 500k-particle sphere morphed
+    """The control-optimisation episode end to end: a 500k-particle sphere morphed
     towards targets displaced by seeded real spherical harmonics (l <= 4),
     one episode per target.  Each episode is run_optimization
     (OptimizeDefGradControlSequence) over 200 steps per pass, control stride

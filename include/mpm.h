@@ -169,7 +169,7 @@ int mpm_winding_numbers(int n_points, const float* points, int n_tris, const flo
 int mpm_compgraph_create(const mpm_pointcloud* pc, const mpm_grid* grid, mpm_grid* target_grid,
                          const mpm_options* opt, mpm_compgraph** out);
 int mpm_compgraph_release(mpm_compgraph* cg);
-/* No counterpart in the reference (BASELINE configuration 3): a CompGraph
+/* No counterpart in the reference: a CompGraph
  * over `count` independent instances, each with its own particles and grid
  * (uneven sizes allowed), advanced together -- every kernel launch covers
  * all instances through per-instance particle and node offsets.  dt, drag,

@@ -6,7 +6,7 @@
   DiffMPMLib3D sources compiled together with ``ref_driver.cpp``.  Built only
   where the reference tree is present (``REF_DIR``, default the read-only
   mount).  The sources are read where they lie; the FP64 variant and the
-  ``private:`` -> ``public:`` edit (so the driver can set CompGraph's dt, drag
+  ``private:`` -> ``public:`` edit (so ``ref_driver.cpp`` can set CompGraph's dt, drag
   and smoothing) are applied to temporary copies outside this repository.
   Only the two shared libraries are written into ``oracle/_ref/``.
 

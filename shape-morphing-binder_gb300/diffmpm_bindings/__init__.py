@@ -332,7 +332,7 @@ class CompGraph:
     def batch(cls, point_clouds, grids, *, adjoint="reference", kernel="cubic", material="fcr",
               checkpoint_every=1, deterministic=False) -> "CompGraph":
         """Independent instances advanced together in one launch per kernel
-        (additive; BASELINE configuration 3).  ``instance_range(i)`` gives the
+        (additive).  ``instance_range(i)`` gives the
         slice of instance i in the concatenated layer arrays."""
         if len(point_clouds) != len(grids) or not point_clouds:
             raise RuntimeError("batch needs one grid per point cloud")

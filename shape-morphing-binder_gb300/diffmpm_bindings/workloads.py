@@ -1,24 +1,24 @@
-"""Seeded synthetic particle sets for the five benchmark configurations.
+"""Seeded synthetic particle sets for the benchmark workloads.
 
 The reference ships no benchmark inputs; these generators stand in for them
-with the shapes, sizes and value distributions of the configurations:
+with the workloads' shapes, sizes and value distributions:
 
-1. ``sphere32``    sphere r=0.25 in the unit cube, 8 particles per cell,
-                   33^3 nodes (dx=1/32), E=1e4, nu=0.3, dt=1e-3, 20 steps.
-2. ``ellipsoid64`` ellipsoid semi-axes (0.35,0.25,0.2), 8 ppc, 65^3 nodes
-                   (dx=1/64), E=5e4, nu=0.35, dt=5e-4, 100 steps, checkpoint 10.
-3. ``batched``     64 randomly scaled/rotated ellipsoids, N log-uniform in
-                   [5k,200k], grids 32^3..96^3, E log-U[1e3,1e5], nu U[0.2,0.45].
-4. ``spheres2m``   union of 8 spheres r in [0.08,0.15], exactly N particles
-                   (default 2M) on 129^3 nodes, 400 steps, checkpoint 20.
-5. ``morph500k``   500k-particle sphere and a target displaced by seeded
-                   real spherical harmonics of degree <= 4.
+* ``sphere32``    sphere r=0.25 in the unit cube, 8 particles per cell,
+                  33^3 nodes (dx=1/32), E=1e4, nu=0.3, dt=1e-3, 20 steps.
+* ``ellipsoid64`` ellipsoid semi-axes (0.35,0.25,0.2), 8 ppc, 65^3 nodes
+                  (dx=1/64), E=5e4, nu=0.35, dt=5e-4, 100 steps, checkpoint 10.
+* ``batched``     64 randomly scaled/rotated ellipsoids, N log-uniform in
+                  [5k,200k], grids 32^3..96^3, E log-U[1e3,1e5], nu U[0.2,0.45].
+* ``spheres2m``   union of 8 spheres r in [0.08,0.15], exactly N particles
+                  (default 2M) on 129^3 nodes, 400 steps, checkpoint 20.
+* ``morph500k``   500k-particle sphere and a target displaced by seeded
+                  real spherical harmonics of degree <= 4.
 
 Particle mass and volume follow GeometryLoading.cpp:122-140
 (m = rho * pdx^3, vol = pdx^3 with pdx^3 = dx^3 / ppc).  Densities default to
 values that keep the explicit step inside its CFL limit (c*dt/dx <= 0.5);
-the nominal rho=1 diverges for configurations 1-2 (p-wave speed
-sqrt((lam+2mu)/rho) ~ 116 for configuration 1).
+the nominal rho=1 diverges for sphere32 and ellipsoid64 (p-wave speed
+sqrt((lam+2mu)/rho) ~ 116 for sphere32).
 """
 from __future__ import annotations
 
@@ -170,7 +170,7 @@ def spheres2m(seed=3, n=2_000_000, G=128, rho=None, v_amp=0.5, sort=True, steps=
 
 
 def batched(seed=2, count=64, steps=50):
-    """Configuration 3: independent instances of uneven size (list of Workloads)."""
+    """Independent instances of uneven size (list of Workloads)."""
     rng = np.random.default_rng(seed)
     out = []
     dt = 2e-4
@@ -227,7 +227,7 @@ def _real_sph_harm(l, m, theta, phi):
 
 
 def morph500k(seed=4, n=500_000, G=96, episode=0, amp=0.04, rho=None, sort=True) -> Workload:
-    """Configuration 5: sphere -> sphere displaced by seeded real SH noise (l<=4)."""
+    """500k-particle sphere -> sphere displaced by seeded real SH noise (l<=4)."""
     rng = np.random.default_rng(seed)
     dx = 1.0 / G
     E, nu, dt = 1e4, 0.3, 5e-4

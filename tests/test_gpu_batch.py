@@ -1,4 +1,4 @@
-"""Batched instances (BASELINE configuration 3): independent simulations of
+"""Batched instances: independent simulations of
 uneven particle count, grid size and material advanced in one launch per
 kernel must give each instance the result it gets alone."""
 import numpy as np

@@ -1,6 +1,6 @@
 """Gradients of a long checkpointed rollout against central finite
-differences of the FP64 oracle (a down-scaled twin of BASELINE
-configuration 4: a union of 8 seeded spheres, 40 steps, checkpoint every 20
+differences of the FP64 oracle (a down-scaled twin of the 2M-particle
+rollout: a union of 8 seeded spheres, 40 steps, checkpoint every 20
 steps with recomputation, exact adjoint).
 
 The gradient with respect to the layer-0 control dFc, the initial velocity

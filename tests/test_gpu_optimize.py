@@ -76,8 +76,8 @@ def test_more_passes(dm, golden_opt):
     assert h5[-1] <= h3[-1]
 
 
-def test_configuration5_twin_loss_curve(dm, orc):
-    """A down-scaled twin of configuration 5 (sphere -> spherical-harmonic
+def test_control_episode_twin_loss_curve(dm, orc):
+    """A down-scaled twin of the 500k-particle control-optimisation episode (sphere -> spherical-harmonic
     target, deterministic scatters, FP64 Adam moments): the FP32 engine's loss
     curve against the FP64 oracle's, evaluation by evaluation."""
     import oracle as O
