@@ -394,7 +394,7 @@ def run_morph(args, device):
     f1, b1 = dm.step_count()
     psteps = n * ((f1 - f0) + (b1 - b0))
     return {
-        "metric": "configuration-5 optimisation, particle-steps/s end to end", "value": round(psteps / total, 1),
+        "metric": "control-optimisation episode (500k-particle sphere morph), particle-steps/s end to end", "value": round(psteps / total, 1),
         "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "seconds_per_episode": round(total / max(1, args.steps), 3), "seconds_total": round(total, 3),
         "higher_is_better": True, "dtype": "f32 (FP64-guarded stress, FP64 Adam moments)",
@@ -410,7 +410,7 @@ def run_morph(args, device):
 
 def run_render(args, device):
     """The Gaussian rasterizer (diff_gauss) on the particles of the
-    configuration-5 sphere: 500k Gaussians (covariance from F = I and half a
+    500k-particle morph sphere: 500k Gaussians (covariance from F = I and half a
     grid spacing), 1024 x 1024, colors precomputed, normals from scale and
     rotation; one step = forward + backward of an image loss.  CUDA events on
     the current stream; the backward includes the host read of the number of
