@@ -271,6 +271,12 @@ int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes,
  * choice (best_ms: one timed forward+backward of the winner; the adjoint
  * budgets: mpm_compgraph_get_adjoint_tiles) */
 int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms);
+/* the same, timing the candidates from the state of `layer` (a stored layer
+ * after a forward pass).  A layer deep in a rollout has drifted from the
+ * cell order of the set-up sort, which favours larger scatter tiles than
+ * layer 0 does. */
+int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* best_tile, int* best_mode,
+                                double* best_ms);
 /* record forward/backward passes as CUDA graphs and replay them (1 = on,
  * the default): a pass is recorded the second time it runs with the same
  * buffers and parameters and replayed from then on */

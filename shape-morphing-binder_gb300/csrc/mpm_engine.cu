@@ -2113,15 +2113,19 @@ int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes,
     });
 }
 
-int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms)
+int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* best_tile, int* best_mode,
+                                double* best_ms)
 {
     return guard([&] {
         check_cg(cg);
         Graph& G = cg->g;
         if (steps < 1) fail(MPM_ERR_ARG, "steps must be positive");
-        if (!G.layers[0].pc || !G.layers[0].pc->have_state) fail(MPM_ERR_STATE, "layer 0 is not stored");
+        if (layer < 0 || layer >= (int)G.layers.size())
+            fail(MPM_ERR_RANGE, "layer %d out of range [0, %d)", layer, (int)G.layers.size());
+        if (!G.layers[layer].pc || !G.layers[layer].pc->have_state)
+            fail(MPM_ERR_STATE, "layer %d holds no state (not stored, or before the forward pass)", layer);
         cudaStream_t s = G.stream;
-        // a scratch copy of the graph: layer 0's state, `steps` steps, full tape
+        // a scratch copy of the graph: that layer's state, `steps` steps, full tape
         Graph T;
         T.prec = G.prec;
         T.opt = G.opt;
@@ -2133,7 +2137,7 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
         T.total_nodes = G.total_nodes;
         T.stream = s;
         T.resort_on = false;  // shares G's constant planes: never permute them from here
-        T.base = clone_pc(*G.layers[0].pc, s, true);
+        T.base = clone_pc(*G.layers[layer].pc, s, true);
         T.base->grads.reset();
         T.layers.resize(1);
         T.layers[0].pc = T.base;
@@ -2211,6 +2215,11 @@ int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* be
         if (best_mode) *best_mode = bm;
         if (best_ms) *best_ms = best;
     });
+}
+
+int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms)
+{
+    return mpm_compgraph_autotune_from(cg, 0, steps, best_tile, best_mode, best_ms);
 }
 
 int mpm_compgraph_use_graphs(mpm_compgraph* cg, int on)

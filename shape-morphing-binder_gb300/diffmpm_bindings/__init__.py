@@ -414,13 +414,16 @@ class CompGraph:
         ptr = getattr(stream, "cuda_stream", stream)
         check(lib.mpm_compgraph_set_stream(self._h, C.c_void_p(ptr) if ptr else None))
 
-    def autotune(self, steps: int = 4) -> dict:
-        """Pick the fastest scatter strategy / node-tile budget for this graph
-        by timing short forward+backward passes (additive)."""
+    def autotune(self, steps: int = 4, layer: int = 0) -> dict:
+        """Pick the fastest scatter strategy and node-tile budgets for this
+        graph by timing short forward+backward passes from the state of
+        `layer` (additive; a stored layer deep in a computed rollout reflects
+        the particle drift of long rollouts)."""
         t, m, ms = C.c_int(), C.c_int(), C.c_double()
-        check(lib.mpm_compgraph_autotune(self._h, int(steps), C.byref(t), C.byref(m), C.byref(ms)), "autotune")
+        check(lib.mpm_compgraph_autotune_from(self._h, int(layer), int(steps), C.byref(t), C.byref(m), C.byref(ms)),
+              "autotune")
         out = self.get_tuning()
-        out.update(ms_per_pass=ms.value, steps=int(steps))
+        out.update(ms_per_pass=ms.value, steps=int(steps), from_layer=int(layer))
         return out
 
     def set_tuning(self, tile_nodes=-1, scatter_mode=-1, adj_tile_nodes=-1, gather_tile_nodes=-1):

@@ -112,6 +112,7 @@ _SIGS = {
     "mpm_step_count": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "mpm_compgraph_get_tuning": [_vp, _ip, _ip],
     "mpm_compgraph_autotune": [_vp, C.c_int, _ip, _ip, _dp],
+    "mpm_compgraph_autotune_from": [_vp, C.c_int, C.c_int, _ip, _ip, _dp],
     "mpm_compgraph_set_adjoint_tiles": [_vp, C.c_int, C.c_int],
     "mpm_compgraph_get_adjoint_tiles": [_vp, _ip, _ip],
     "mpm_compgraph_synchronize": [_vp],

@@ -360,6 +360,19 @@ def test_autotune_picks_a_valid_configuration(dm, orc):
     assert rel_err(cg.get_point_cloud(1).get("x", np.float64), want.x) < 1e-6
 
 
+def test_autotune_from_a_stored_layer(dm):
+    s0, g, rng, _, _ = _case(13, G=12)
+    prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0)
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=5, checkpoint_every=2)
+    cg.compute_forward_pass(0, 0)
+    res = cg.autotune(steps=2, layer=2)
+    assert res["from_layer"] == 2 and res["tile_nodes"] in (0, 512, 1024, 2048) and res["ms_per_pass"] > 0
+    with pytest.raises(IndexError):
+        cg.autotune(steps=2, layer=9)
+    with pytest.raises(RuntimeError, match="no state"):  # layer 3 is not stored (checkpoint every 2)
+        cg.autotune(steps=2, layer=3)
+
+
 def test_adjoint_tile_budgets_change_no_result(dm):
     """The adjoint kernels' own tile budgets (or tiles off): the P2G
     transpose's gather reads the same node values from the tile as from
