@@ -14,7 +14,6 @@ Additive API (not in the reference): ``PointCloud.from_arrays``,
 from __future__ import annotations
 
 import ctypes as C
-import math
 
 import numpy as np
 

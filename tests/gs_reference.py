@@ -13,7 +13,6 @@ with.  Small scenes only.
 """
 from __future__ import annotations
 
-import math
 
 import torch
 

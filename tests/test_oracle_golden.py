@@ -2,7 +2,6 @@
 sources (tests/golden/reference_small.npz, made by tests/golden/make_golden.py
 from DiffMPMLib3D compiled with float widened to double)."""
 import numpy as np
-import pytest
 
 import oracle as O
 from helpers import golden_grid, golden_params, golden_state, rel_err
