@@ -533,6 +533,18 @@ struct Graph {
     std::shared_ptr<PCData> ping, pong;             // non-stored forward states
     std::vector<std::shared_ptr<PCData>> seg;       // recomputed segment states
     std::vector<Buf> sgrid, strust;                 // recomputed segment grids
+    // The last checkpoint segment [lo, hi] as the forward pass computed it:
+    // states of layers lo+1..hi-1 in seg[1..], step grids and trust scales
+    // in sgrid/strust.  The backward pass starts with this segment, so it
+    // takes them instead of recomputing, while they are still valid: no
+    // state written since (g_state_epoch), the same step configuration, and
+    // no other segment recomputed into the scratch since.
+    struct Tail {
+        bool valid = false;
+        int lo = -1, hi = -1;
+        unsigned long long epoch = 0;
+        std::vector<unsigned long long> cfg;
+    } tail;
     bool lame_on = false;                           // accumulate dL/dlam, dL/dmu
     Buf glame;                                      // 2 planes
     // captured forward/backward passes, keyed by pass and start layer
@@ -697,6 +709,9 @@ void check_fix(Graph& G, bool raise = true)
 }
 
 long long g_fwd_steps = 0, g_bwd_steps = 0;  // particle-layer steps executed (host count)
+// bumped by every host write of particle state or constants, and by every
+// operation that changes a graph's layers outside its own passes
+unsigned long long g_state_epoch = 0;
 
 // Re-sort the graph's particles by (instance, cell) of layer 0's positions:
 // every particle plane of every layer (state, constants, control, gradients,
@@ -705,6 +720,7 @@ long long g_fwd_steps = 0, g_bwd_steps = 0;  // particle-layer steps executed (h
 template <typename R>
 void graph_resort(Graph& G)
 {
+    ++g_state_epoch;
     PCData& d0 = *G.layers[0].pc;
     if (!d0.have_state || d0.n <= 1) return;
     cudaStream_t s = G.stream;
@@ -986,20 +1002,44 @@ void graph_forward(Graph& G, int start)
     sig.add_pc(G.pong.get());
     sig.add(G.fgrid);
     sig.add(G.ftrust);
+    // checkpointed: the last segment's states, grids and trust scales go to
+    // the segment scratch, where the backward pass will look for them
+    const int k = std::max(1, G.opt.checkpoint_every);
+    const int tail_lo = full ? -1 : ((L - 2) / k) * k;
+    const bool keep_tail = !full && L >= 2 && tail_lo >= start;
+    if (keep_tail) {
+        const int cnt = L - tail_lo;
+        if ((int)G.seg.size() < cnt) G.seg.resize(cnt);
+        if ((int)G.sgrid.size() < cnt) {
+            G.sgrid.resize(cnt);
+            G.strust.resize(cnt);
+        }
+    }
+    for (auto& q : G.seg) sig.add_pc(q.get());
+    for (auto& b : G.sgrid) sig.add(b);
+    for (auto& b : G.strust) sig.add(b);
+    G.tail.valid = false;
     run_captured(G, "fwd" + std::to_string(start), sig, [&]() {
         PCData* cur = G.layers[start].pc.get();
         begin_fix_pass(G, c, *cur, s);
         for (int i = start; i < L - 1; ++i) {
             PCData* nxt;
+            const bool in_tail = keep_tail && i >= tail_lo;
             if (G.stored(i + 1)) {
                 nxt = G.layers[i + 1].pc.get();
                 if (!nxt->st) nxt->st = make_buf(cur->planes_bytes(ST_N), s, false);
+            } else if (in_tail) {
+                auto& q = G.seg[i + 1 - tail_lo];
+                const PCData& lo_pc = *G.layers[tail_lo].pc;
+                if (!q || q->n != lo_pc.n) q = shell_like(lo_pc, s, true);
+                nxt = q.get();
             } else {
                 auto& tmp = (cur == G.ping.get()) ? G.pong : G.ping;
                 if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
                 nxt = tmp.get();
             }
             if (full) step_forward<R>(c, *cur, *nxt, G.layers[i].grid, G.layers[i].trust, s);
+            else if (in_tail) step_forward<R>(c, *cur, *nxt, G.sgrid[i - tail_lo], G.strust[i - tail_lo], s);
             else step_forward<R>(c, *cur, *nxt, G.fgrid, G.ftrust, s);
             cur = nxt;
         }
@@ -1010,6 +1050,15 @@ void graph_forward(Graph& G, int start)
             G.layers[i].pc->dfc_zero = true;
             G.layers[i].pc->have_state = true;
         }
+    if (keep_tail) {
+        Sig cs;
+        cs.add_cfg(c);
+        G.tail.valid = true;
+        G.tail.lo = tail_lo;
+        G.tail.hi = L - 1;
+        G.tail.epoch = g_state_epoch;
+        G.tail.cfg = cs.v;
+    }
 }
 
 template <typename R>
@@ -1038,7 +1087,7 @@ void inject_render_grads(Graph& G)
 }
 
 template <typename R>
-void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s);
+void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s, bool tail_ok);
 
 // ComputeBackwardPass (CompGraph.cpp:143-211).  With checkpointing each
 // segment [lo, hi] between stored layers is recomputed from lo (states, grids
@@ -1075,6 +1124,14 @@ void graph_backward(Graph& G, int control)
     for (auto& q : G.seg) sig.add_pc(q.get());
     for (auto& b : G.sgrid) sig.add(b);
     for (auto& b : G.strust) sig.add(b);
+    bool tail_ok = false;
+    if (k > 1 && G.tail.valid && G.tail.hi == L - 1 && G.tail.lo == ((L - 2) / k) * k &&
+        G.tail.epoch == g_state_epoch) {
+        Sig cs;
+        cs.add_cfg(c);
+        tail_ok = cs.v == G.tail.cfg;
+    }
+    sig.add((unsigned long long)tail_ok);
     run_captured(G, "bwd" + std::to_string(control), sig, [&]() {
         if (G.lame_on) ck(cudaMemsetAsync(G.glame->p, 0, G.glame->bytes, s), "memset");
         begin_fix_pass(G, c, *G.layers[control].pc, s);
@@ -1085,12 +1142,14 @@ void graph_backward(Graph& G, int control)
             }
             return;
         }
-        backward_segments<R>(G, c, control, L, k, s);
+        backward_segments<R>(G, c, control, L, k, s, tail_ok);
     });
+    // recomputing an earlier segment overwrites the scratch
+    if (k > 1 && control < ((L - 2) / k) * k) G.tail.valid = false;
 }
 
 template <typename R>
-void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s)
+void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s, bool tail_ok)
 {
     int hi = L - 1;
     while (hi > control) {
@@ -1109,9 +1168,12 @@ void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cu
             S[j] = G.seg[j].get();
         }
         if (!G.ping || G.ping->n != S[0]->n) G.ping = shell_like(*S[0], s, true);
-        for (int j = 0; j < cnt - 1; ++j) {
-            PCData* out = (j + 1 < cnt - 1) ? S[j + 1] : G.ping.get();
-            step_forward<R>(c, *S[j], *out, G.sgrid[j], G.strust[j], s);
+        // the last segment, as the forward pass left it, needs no recompute
+        if (!(tail_ok && hi == L - 1)) {
+            for (int j = 0; j < cnt - 1; ++j) {
+                PCData* out = (j + 1 < cnt - 1) ? S[j + 1] : G.ping.get();
+                step_forward<R>(c, *S[j], *out, G.sgrid[j], G.strust[j], s);
+            }
         }
         const int stop = std::max(control, lo);
         for (int i = hi - 1; i >= stop; --i) {
@@ -1222,6 +1284,7 @@ template <typename R>
 void graph_set_up(Graph& G, int num_layers)
 {
     if (num_layers <= 0) fail(MPM_ERR_ARG, "num_layers must be positive");
+    G.tail.valid = false;
     cudaStream_t s = G.stream;
     if (G.resort_on) {
         // the other layers are rebuilt from layer 0 below: sort layer 0 only
@@ -1453,6 +1516,7 @@ int mpm_pointcloud_set(mpm_pointcloud* pc, int field, const void* src, int dtype
     return guard([&] {
         check_pc(pc);
         if (!src && pc->d->n) fail(MPM_ERR_ARG, "null source");
+        if (field < MPM_FIELD_GRAD_X) ++g_state_epoch;  // state or constants: kept segments go stale
         with_prec(pc->d->prec, [&](auto r) {
             using R = decltype(r);
             pc_set<R>(*pc->d, field, src, dtype, on_device, pc->stream);
@@ -1926,6 +1990,7 @@ int mpm_compgraph_promote_last_as_initial(mpm_compgraph* cg, int carry_grid)
     return guard([&] {
         check_cg(cg);
         Graph& G = cg->g;
+        ++g_state_epoch;
         if (G.layers.empty()) return;
         if (!G.layers.back().pc->have_state) fail(MPM_ERR_STATE, "last layer not stored");
         G.layers.front().pc = G.layers.back().pc;
@@ -1949,6 +2014,7 @@ int mpm_compgraph_adam_step(mpm_compgraph* cg, int layer, double alpha, double g
     return guard([&] {
         check_cg(cg);
         if (layer < 0 || layer >= (int)cg->g.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
+        ++g_state_epoch;  // the control changes
         with_prec(cg->g.prec, [&](auto r) { graph_adam<decltype(r)>(cg->g, layer, alpha, gnorm, b1, b2, eps, timestep); });
         ck(cudaStreamSynchronize(cg->g.stream), "adam");
     });

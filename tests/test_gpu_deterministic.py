@@ -163,3 +163,41 @@ def test_deterministic_launch_count(dm):
     n0 = lib.mpm_launch_count()
     cg.compute_forward_pass(0, 0)  # a replay counts what it replays
     assert lib.mpm_launch_count() - n0 == 3 * T + 1  # + the mass-scale kernel
+
+
+def test_checkpoint_tail_kept_from_the_forward_pass(dm):
+    """The backward pass takes the last checkpoint segment (states, grids,
+    trust scales) from the forward pass instead of recomputing it, unless a
+    state write came in between.  Either way the gradients are the same bits."""
+    s0, g, rng = _case(7)
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.05, exact=True)
+    T, k = 9, 3
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    cg, keep = make_graph(dm, s0, g, prm, precision="fp32", adjoint="exact", layers=T + 1, checkpoint_every=k,
+                          deterministic=True)
+
+    def backward():
+        cg.get_point_cloud(T).set("grad_x", seed_gx)
+        f0, b0 = dm.step_count()
+        cg.compute_backward_pass(0)
+        f1, b1 = dm.step_count()
+        assert b1 - b0 == T
+        return f1 - f0, {key: cg.get_grad(0, key, np.float32) for key in ("x", "v", "F", "dFc")}
+
+    cg.compute_forward_pass(0, 0)
+    fwd_kept, g_kept = backward()
+    assert fwd_kept == T - k  # segments [0,3] and [3,6] recomputed, [6,9] kept
+    cg.compute_forward_pass(0, 0)
+    cg.get_point_cloud(0).set("v", s0.v)  # the same values: a state write all the same
+    fwd_redo, g_redo = backward()
+    assert fwd_redo == T
+    for key in g_kept:
+        assert np.array_equal(g_kept[key], g_redo[key]), key
+    # two backward passes after one forward: the first keeps the tail, then
+    # overwrites the scratch with segments [3,6] and [0,3]; the second recomputes
+    cg.compute_forward_pass(0, 0)
+    assert backward()[0] == T - k
+    fwd_again, g_again = backward()
+    assert fwd_again == T
+    for key in g_kept:
+        assert np.array_equal(g_kept[key], g_again[key]), key
