@@ -382,6 +382,8 @@ static long long n_nodes(const orc_grid *G) { return (long long)G->dims[0] * G->
                 long long node_ = ((long long)i_ * (G)->dims[1] + j_) * (G)->dims[2] + k_;  \
                 double w_ = (st).w[0][a_] * (st).w[1][b_] * (st).w[2][c_];                \
                 double dg_[3] = {(st).g[0][a_], (st).g[1][b_], (st).g[2][c_]};            \
+                (void)w_;                                                                 \
+                (void)dg_;                                                                \
                 __VA_ARGS__                                                               \
             }                                                                             \
         }                                                                                 \
