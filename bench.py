@@ -598,6 +598,23 @@ def cpu_sample(w, particles: int, T: int):
     return s, g, prm, seed
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo, else lscpu), for the CPU legs."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_baseline(w, args):
     import build_oracle
     build_oracle.build_oracle()
@@ -609,7 +626,7 @@ def cpu_baseline(w, args):
     t0 = time.perf_counter()
     orc.rollout(g, prm, s, T, seed)
     dt = time.perf_counter() - t0
-    return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "kind": "port",
+    return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "cpu": cpu_model(), "kind": "port",
             "sample": f"{s.n} of {w.n} particles of {w.name}, {T} timestep(s) forward + reference adjoint, "
                       f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)"}
 
