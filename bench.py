@@ -626,9 +626,26 @@ def cpu_baseline(w, args):
     t0 = time.perf_counter()
     orc.rollout(g, prm, s, T, seed)
     dt = time.perf_counter() - t0
+    # the same sample again step by step, forward and adjoint timed apart
+    try:
+        t1 = time.perf_counter()
+        states, steps = [s], []
+        for _ in range(T):
+            s1, st = orc.forward_step(g, prm, states[-1])
+            states.append(s1)
+            steps.append(st)
+        t2 = time.perf_counter()
+        gg = O.Grads(seed, np.zeros((s.n, 3)), np.zeros((s.n, 3, 3)), np.zeros((s.n, 3, 3)))
+        for t in range(T - 1, -1, -1):
+            gg = orc.backward_step(g, prm, states[t], states[t + 1].C, steps[t], gg)
+        t3 = time.perf_counter()
+        split = {"forward_s": round(t2 - t1, 3), "backward_s": round(t3 - t2, 3)}
+    except Exception as e:  # the split is a detail; the measured value stands without it
+        split = {"split_error": str(e)[:120]}
     return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "cpu": cpu_model(), "kind": "port",
             "sample": f"{s.n} of {w.n} particles of {w.name}, {T} timestep(s) forward + reference adjoint, "
-                      f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)"}
+                      f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)",
+            **split}
 
 
 def run_reference(args, rank, world):
