@@ -615,18 +615,8 @@ def cpu_model() -> str:
     return platform.machine()
 
 
-def cpu_baseline(w, args):
-    import build_oracle
-    build_oracle.build_oracle()
-    import oracle as O
-    orc = O.Oracle()
-    particles = args.cpu_particles or w.n
-    T = args.cpu_timesteps
-    s, g, prm, seed = cpu_sample(w, particles, T)
-    t0 = time.perf_counter()
-    orc.rollout(g, prm, s, T, seed)
-    dt = time.perf_counter() - t0
-    # the same sample again step by step, forward and adjoint timed apart
+def cpu_split(orc, O, g, prm, s, T, seed) -> dict:
+    """The CPU sample again, step by step: forward and adjoint timed apart."""
     try:
         t1 = time.perf_counter()
         states, steps = [s], []
@@ -639,13 +629,27 @@ def cpu_baseline(w, args):
         for t in range(T - 1, -1, -1):
             gg = orc.backward_step(g, prm, states[t], states[t + 1].C, steps[t], gg)
         t3 = time.perf_counter()
-        split = {"forward_s": round(t2 - t1, 3), "backward_s": round(t3 - t2, 3)}
-    except Exception as e:  # the split is a detail; the measured value stands without it
-        split = {"split_error": str(e)[:120]}
+        return {"forward_s": round(t2 - t1, 3), "backward_s": round(t3 - t2, 3)}
+    except Exception as e:  # a detail of the report; the measured value stands without it
+        return {"split_error": str(e)[:120]}
+
+
+def cpu_baseline(w, args, split=True):
+    import build_oracle
+    build_oracle.build_oracle()
+    import oracle as O
+    orc = O.Oracle()
+    particles = args.cpu_particles or w.n
+    T = args.cpu_timesteps
+    s, g, prm, seed = cpu_sample(w, particles, T)
+    t0 = time.perf_counter()
+    orc.rollout(g, prm, s, T, seed)
+    dt = time.perf_counter() - t0
+    extra = cpu_split(orc, O, g, prm, s, T, seed) if split else {}
     return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "cpu": cpu_model(), "kind": "port",
             "sample": f"{s.n} of {w.n} particles of {w.name}, {T} timestep(s) forward + reference adjoint, "
                       f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)",
-            **split}
+            **extra}
 
 
 def run_reference(args, rank, world):
@@ -655,7 +659,7 @@ def run_reference(args, rank, world):
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, args)
+        cb = cpu_baseline(w, args, split=(i == args.warmup + args.steps - 1))
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals)) if vals else cb["value"]
