@@ -59,3 +59,6 @@ def test_reference_arm_under_torchrun():
     import json
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0 and d["cpu_baseline"]["kind"] == "port"
+    cb = d["cpu_baseline"]
+    assert cb["cores"] >= 1 and cb["cpu"] and cb["forward_s"] > 0 and cb["backward_s"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
