@@ -330,6 +330,7 @@ def run_ours(args, rank, world, device):
                                                                     else "")},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
         "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
+        "native_libs": native_libs(),
     }
     if fp64:
         line["fp64_plain"] = fp64
@@ -634,7 +635,26 @@ def cpu_split(orc, O, g, prm, s, T, seed) -> dict:
         return {"split_error": str(e)[:120]}
 
 
-def cpu_baseline(w, args, split=True):
+def cpu_single_thread(orc, O, w, particles: int, T: int) -> dict:
+    """The same algorithm on one host thread, over a smaller sample (an
+    eighth of the particles): the reference's adjoint serialises its G2P
+    transpose (BackPropagation.cpp:50-53), so its one-thread figure is the
+    other number a reader needs."""
+    threads = orc.threads()
+    sub = max(1, particles // 8)
+    s, g, prm, seed = cpu_sample(w, sub, T)
+    try:
+        orc.set_threads(1)
+        t0 = time.perf_counter()
+        orc.rollout(g, prm, s, T, seed)
+        dt = time.perf_counter() - t0
+    finally:
+        orc.set_threads(threads)
+    return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": 1,
+            "sample": f"{s.n} of {w.n} particles, {T} timestep(s) forward + reference adjoint"}
+
+
+def cpu_baseline(w, args, split=True, single=True):
     import build_oracle
     build_oracle.build_oracle()
     import oracle as O
@@ -646,10 +666,26 @@ def cpu_baseline(w, args, split=True):
     orc.rollout(g, prm, s, T, seed)
     dt = time.perf_counter() - t0
     extra = cpu_split(orc, O, g, prm, s, T, seed) if split else {}
+    if single:
+        extra["single_thread"] = cpu_single_thread(orc, O, w, particles, T)
     return {"value": round(s.n * T / dt, 1), "unit": UNIT, "cores": orc.threads(), "cpu": cpu_model(), "kind": "port",
             "sample": f"{s.n} of {w.n} particles of {w.name}, {T} timestep(s) forward + reference adjoint, "
                       f"full {w.dims[0]}^3 grid, FP64 CPU restatement (oracle/mpm_oracle.c, OpenMP)",
             **extra}
+
+
+def native_libs() -> list[str]:
+    """Shared libraries of this repository mapped into this process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.endswith(".so") and path.startswith(str(ROOT)):
+                    out.add(str(Path(path).relative_to(ROOT)))
+    except OSError:
+        pass
+    return sorted(out)
 
 
 def run_reference(args, rank, world):
@@ -659,7 +695,8 @@ def run_reference(args, rank, world):
     vals = []
     cb = None
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, args, split=(i == args.warmup + args.steps - 1))
+        last = i == args.warmup + args.steps - 1
+        cb = cpu_baseline(w, args, split=last, single=last)
         if i >= args.warmup:
             vals.append(cb["value"])
     v = float(np.mean(vals)) if vals else cb["value"]
@@ -670,7 +707,8 @@ def run_reference(args, rank, world):
             "config": {"workload": w.name, "particles": w.n, "timesteps": w.steps,
                        "note": "reference CPU path (restated in oracle/, OpenMP); each step is a bounded sample"},
             "cpu_baseline": cb, "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}
+                                        "d2h_bytes_per_step": 0},
+            "native_libs": native_libs()}
 
 
 # ------------------------------------------------------------ distributed

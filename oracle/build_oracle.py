@@ -4,13 +4,15 @@
   (gcc + OpenMP).  Built on every machine that runs the tests.
 * ``oracle/_ref/libref32.so`` / ``libref64.so`` -- the reference's own
   DiffMPMLib3D sources compiled together with ``ref_driver.cpp``.  Built only
-  where the reference tree is present (``REF_DIR``, default the read-only
-  mount).  The sources are read where they lie; the FP64 variant and the
-  ``private:`` -> ``public:`` edit (so ``ref_driver.cpp`` can set CompGraph's dt, drag
-  and smoothing) are applied to temporary copies outside this repository.
-  Only the two shared libraries are written into ``oracle/_ref/``.
+  where the reference tree is named by the ``REF_DIR`` environment variable
+  (the checkout's root, holding ``DiffMPMLib3D/`` and ``include/``); without
+  it they are skipped and the tests that need them skip too.  The sources
+  are read where they lie; the FP64 variant and the ``private:`` ->
+  ``public:`` edit (so ``ref_driver.cpp`` can set CompGraph's dt, drag and
+  smoothing) are applied to temporary copies outside this repository.  Only
+  the two shared libraries are written into ``oracle/_ref/``.
 
-Usage: ``python oracle/build_oracle.py [--no-ref] [--force]``
+Usage: ``REF_DIR=<reference checkout> python oracle/build_oracle.py [--no-ref] [--force]``
 """
 from __future__ import annotations
 
@@ -26,7 +28,13 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT_REF = HERE / "_ref"
-REF_DIR = Path(os.environ.get("REF_DIR", "/root/reference"))
+
+
+def ref_dir() -> Path | None:
+    """The reference checkout named by $REF_DIR, or None."""
+    d = os.environ.get("REF_DIR")
+    return Path(d) if d else None
+
 
 REF_SOURCES = [
     "ForwardSimulation.cpp", "BackPropagation.cpp", "Elasticity.cpp", "PointCloud.cpp",
@@ -67,11 +75,11 @@ def _widen(text: str) -> str:
     return _FLOAT_LIT.sub(r"\1", text)
 
 
-def _stage(tmp: Path, widen: bool) -> Path:
+def _stage(tmp: Path, widen: bool, ref: Path) -> Path:
     """Copy DiffMPMLib3D into tmp with the mechanical edits applied."""
     dst = tmp / ("src64" if widen else "src32")
     dst.mkdir(parents=True, exist_ok=True)
-    for f in (REF_DIR / "DiffMPMLib3D").iterdir():
+    for f in (ref / "DiffMPMLib3D").iterdir():
         if f.suffix not in (".h", ".cpp"):
             continue
         text = f.read_text(encoding="utf-8", errors="replace")
@@ -89,11 +97,12 @@ def _compile(args):
 
 
 def build_ref(force: bool = False) -> list[Path]:
-    if not (REF_DIR / "DiffMPMLib3D" / "ForwardSimulation.cpp").exists():
+    ref = ref_dir()
+    if ref is None or not (ref / "DiffMPMLib3D" / "ForwardSimulation.cpp").exists():
         return []
     OUT_REF.mkdir(exist_ok=True)
     outs = []
-    inputs = [HERE / "ref_driver.cpp", Path(__file__)] + [REF_DIR / "DiffMPMLib3D" / s for s in REF_SOURCES]
+    inputs = [HERE / "ref_driver.cpp", Path(__file__)] + [ref / "DiffMPMLib3D" / s for s in REF_SOURCES]
     todo = []
     for widen, name in ((False, "libref32.so"), (True, "libref64.so")):
         out = OUT_REF / name
@@ -106,8 +115,8 @@ def build_ref(force: bool = False) -> list[Path]:
     try:
         jobs, links = [], []
         for widen, out in todo:
-            src = _stage(tmp, widen)
-            inc = ["-I", str(src), "-I", str(REF_DIR / "include"), "-I", str(REF_DIR / "include" / "qrsvd")]
+            src = _stage(tmp, widen, ref)
+            inc = ["-I", str(src), "-I", str(ref / "include"), "-I", str(ref / "include" / "qrsvd")]
             objs = []
             for s in REF_SOURCES + ["ref_driver.cpp"]:
                 cpp = (HERE / s) if s == "ref_driver.cpp" else (src / s)

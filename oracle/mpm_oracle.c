@@ -920,3 +920,16 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/* Threads the OpenMP loops above use from now on (n >= 1); the CPU-baseline
+ * legs time the reference algorithm on all host threads and on one, since
+ * the reference's adjoint serialises its G2P transpose (omp critical,
+ * BackPropagation.cpp:50-53) and runs no faster on many threads. */
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n >= 1) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

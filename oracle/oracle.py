@@ -159,6 +159,10 @@ class Oracle:
     def threads(self) -> int:
         return self.lib.orc_num_threads()
 
+    def set_threads(self, n: int) -> None:
+        """OpenMP threads of the following calls (the process-wide setting)."""
+        self.lib.orc_set_threads(C.c_int(int(n)))
+
     # -- constitutive
     def pk(self, F, lam, mu, material=0):
         F = _f64(F, (3, 3))

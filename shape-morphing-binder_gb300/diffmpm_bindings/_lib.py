@@ -1,7 +1,10 @@
 """ctypes binding of libmpm.so (the C ABI in include/mpm.h).
 
 The library is built in-tree by ``shape-morphing-binder_gb300/build.py``.
-Loading fails loudly when it is missing: there is no CPU fallback.
+It is opened on first use (the first call through ``lib``), so importing the
+package -- e.g. for its numpy-only workload generators -- maps no native
+code.  Opening fails loudly when the library is missing: there is no CPU
+fallback.
 """
 from __future__ import annotations
 
@@ -147,10 +150,34 @@ def _load() -> C.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = _RESTYPE.get(name, C.c_int)
+    if os.environ.get("MPM_QUIET"):
+        lib.mpm_set_verbose(0)
     return lib
 
 
-lib = _load()
+class _LazyLib:
+    """libmpm.so, opened by the first attribute lookup (a C entry point).
+
+    Each entry point is cached on this object after its first lookup, so
+    later calls cost one attribute access, as with a plain ctypes.CDLL."""
+
+    def __init__(self):
+        self._cdll = None
+
+    def loaded(self) -> bool:
+        return self._cdll is not None
+
+    def __getattr__(self, name):
+        if name.startswith("__"):
+            raise AttributeError(name)
+        if self._cdll is None:
+            self._cdll = _load()
+        fn = getattr(self._cdll, name)
+        setattr(self, name, fn)
+        return fn
+
+
+lib = _LazyLib()
 
 
 def check(rc: int, what: str = ""):
@@ -165,6 +192,3 @@ def check(rc: int, what: str = ""):
 def exported_symbols() -> list[str]:
     return sorted(_SIGS)
 
-
-if os.environ.get("MPM_QUIET"):
-    lib.mpm_set_verbose(0)

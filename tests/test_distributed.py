@@ -62,3 +62,8 @@ def test_reference_arm_under_torchrun():
     cb = d["cpu_baseline"]
     assert cb["cores"] >= 1 and cb["cpu"] and cb["forward_s"] > 0 and cb["backward_s"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+    st = cb["single_thread"]
+    assert st["cores"] == 1 and st["value"] > 0
+    # the reference arm runs the CPU restatement only: none of this
+    # repository's engine or kernels is mapped into its process
+    assert d["native_libs"] == ["oracle/liboracle.so"], d["native_libs"]
