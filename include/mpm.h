@@ -304,24 +304,28 @@ int mpm_compgraph_synchronize(mpm_compgraph* cg);
 /* ------------------------------------------------- allocation-free variant */
 /* No counterpart in the reference.  The end-layer mass loss of
  * mpm_compgraph_mass_loss (EndLayerMassLoss, FP32, cubic kernel) for callers
- * that cannot allocate device memory: code that runs inside a fixed memory
- * budget it must not grow, in a host callback or other context where
- * cudaMalloc is not allowed, or under a host runtime that owns every device
- * allocation.  The caller passes device buffers: x (n,3) and m (n) particle
- * positions and masses, target_mass (nx*ny*nz) node masses; dLdx (n,3)
- * receives dL/dx and *loss (host) the loss.  exact = 1 selects the exact
- * derivative of the loss, 0 the reference's own.  The function calls no
- * cudaMalloc, cudaFree or other allocating routine: its scratch (grid mass,
- * dL/dm, FP64 sums) is a file-scope __device__ array of
- * 256 + 8 * MPM_NOALLOC_MAX_NODES bytes (about 8 MB) that every GPU loading
- * the library holds until the process exits.  Grids with more than
- * MPM_NOALLOC_MAX_NODES nodes are rejected with MPM_ERR_SHAPE.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress,
- * with that device current); make that first call before any stream
- * capture.  All calls share the one array, which keeps the previous call's
- * contents (the function clears what it accumulates): calls that overlap on
- * the GPU race.  Work is ordered on `stream` (a cudaStream_t, NULL = legacy
- * default stream); the call returns after the loss has been copied back. */
+ * that cannot allocate device memory: code that must stay inside a fixed
+ * device-memory budget it may not grow, or a host runtime that owns every
+ * device allocation of the process.  The caller passes device buffers: x
+ * (n,3) and m (n) particle positions and masses, target_mass (nx*ny*nz) node
+ * masses; dLdx (n,3) receives dL/dx and *loss (host) the loss.  exact = 1
+ * selects the exact derivative of the loss, 0 the reference's own.  The
+ * function calls no cudaMalloc, cudaFree or other allocating routine: its
+ * scratch (grid mass, dL/dm, FP64 sums) is a file-scope __device__ array of
+ * 256 + 8 * MPM_NOALLOC_MAX_NODES bytes (about 8 MB).  CUDA loads the array
+ * into a device's context with the first call on that device (lazy module
+ * loading, the default), and that first call is where its memory is
+ * allocated; it stays until the context is destroyed.  So make one call per
+ * device ahead of time, outside the restricted context (any valid inputs; n
+ * may be 0), or run the process with CUDA_MODULE_LOADING=EAGER; every later
+ * call allocates nothing.  Grids with more than MPM_NOALLOC_MAX_NODES nodes
+ * are rejected with MPM_ERR_SHAPE.  All calls share the one array, which
+ * keeps the previous call's contents (the function clears what it
+ * accumulates): calls that overlap on the GPU race.  Work is ordered on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call is
+ * synchronous -- it returns after the loss has been copied back -- so it
+ * must not be made from a stream callback (cudaLaunchHostFunc), and a stream
+ * that is being captured is refused with MPM_ERR_STATE. */
 #define MPM_NOALLOC_MAX_NODES (1 << 20)
 int mpm_mass_loss_noalloc(int n, const float* x, const float* m, const float* target_mass, const int* dims,
                           double dx, const double* min_point, int exact, float* dLdx, double* loss, void* stream);

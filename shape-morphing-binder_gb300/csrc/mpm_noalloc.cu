@@ -3,19 +3,26 @@
 // mpm_mass_loss_noalloc() computes the same loss and dL/dx as
 // mpm_compgraph_mass_loss() (the EndLayerMassLoss path), for callers that
 // hand in their own device buffers and cannot allocate device memory
-// themselves or through this library: code running where cudaMalloc is
-// forbidden or unsafe (inside a memory pool's reserved budget, a host callback
-// or a capture-only region), or a host runtime that owns every allocation.
+// themselves or through this library: code that must stay inside a fixed
+// device-memory budget it may not grow (a memory pool reserved up front), or
+// a host runtime that owns every device allocation of the process.
 // Its scratch (the grid mass, dL/dm per node and the four FP64 reduction
-// accumulators) lives in one file-scope __device__ array that every GPU
-// loading this library holds until the process exits.  Every call shares
-// that array: calls that overlap on the GPU (different streams or host
-// threads without ordering) race and give wrong results.
+// accumulators) lives in one file-scope __device__ array.  The array belongs
+// to this file's device code, which CUDA loads into a device's context when
+// the first call on that device touches it (lazy module loading, the
+// default): that first call allocates the module's memory, array included,
+// and the memory stays until the context is destroyed.  Callers therefore
+// make one call per device ahead of time, outside the restricted context
+// (or run with CUDA_MODULE_LOADING=EAGER, which loads it with the library);
+// later calls allocate nothing.  Every call shares the array: calls that
+// overlap on the GPU (different streams or host threads without ordering)
+// race and give wrong results.  The call is synchronous (it copies the loss
+// back and waits for its stream), so it must not be made from a stream
+// callback, and it refuses a stream that is being captured.
 #include <cuda_runtime.h>
 
 #include <climits>
 #include <cmath>
-#include <mutex>
 
 #include "../../include/mpm.h"
 #include "mpm_launch.h"
@@ -29,9 +36,6 @@ constexpr size_t kScratchBytes = kAccBytes + 2 * sizeof(float) * (size_t)kMaxNod
 
 // layout: [acc: 4 doubles | pad][grid mass: kMaxNodes floats][dL/dm: kMaxNodes floats]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
-
-std::mutex g_mu;
-void* g_addr[256] = {nullptr};  // device address of the scratch per device ordinal
 
 struct Geo {
     int dims[3];
@@ -180,28 +184,26 @@ extern "C" int mpm_mass_loss_noalloc(int n, const float* x, const float* m, cons
     if (nn > kMaxNodes) {
         return fail(MPM_ERR_SHAPE, "mpm_mass_loss_noalloc: grid exceeds MPM_NOALLOC_MAX_NODES nodes");
     }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
-        return fail(MPM_ERR_CUDA, "mpm_mass_loss_noalloc: no current CUDA device");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // synchronous call: refuse a stream under capture (the final stream
+    // synchronize would fail and invalidate the caller's capture)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return fail(MPM_ERR_STATE, "mpm_mass_loss_noalloc: the stream is being captured (the call is synchronous)");
     }
-    unsigned char* base = nullptr;
-    {
-        // the host name of a __device__ array is not a device address: look up
-        // the array's address once per device, with that device current
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
-            void* ptr = nullptr;
-            if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
-                return fail(MPM_ERR_CUDA, "mpm_mass_loss_noalloc: cudaGetSymbolAddress failed");
-            }
-            g_addr[dev] = ptr;
-        }
-        base = static_cast<unsigned char*>(g_addr[dev]);
+    // The host name of a __device__ array is not a device address.  The
+    // address is looked up on every call, with the caller's device current:
+    // it is only valid in the context the module is loaded into, which a
+    // device reset or another current context replaces.
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) {
+        return fail(MPM_ERR_CUDA, "mpm_mass_loss_noalloc: cudaGetSymbolAddress failed");
     }
+    unsigned char* base = static_cast<unsigned char*>(ptr);
     double* acc = reinterpret_cast<double*>(base);
     float* gm = reinterpret_cast<float*>(base + kAccBytes);
     float* dLdm = gm + kMaxNodes;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     Geo g;
     for (int a = 0; a < 3; ++a) {
         g.dims[a] = dims[a];

@@ -1,13 +1,15 @@
 """The allocation-free mass loss against the regular one.
 
 mpm_mass_loss_noalloc serves callers that cannot allocate device memory
-(a fixed memory budget, a callback or other context where cudaMalloc is not
-allowed, a host runtime that owns every allocation): it takes the caller's
-device buffers and keeps its own scratch in a static device array.  Here it
-is called through the C ABI twice in a row, on different inputs, and each
-result is compared with mpm_compgraph_mass_loss (CompGraph.end_layer_mass_loss)
-on the same particles: loss within 1e-6 relative, dL/dx within 1e-5 in norm
-(both FP32; only the order of the atomic sums differs).
+(a fixed device-memory budget that may not grow, a host runtime that owns
+every allocation): it takes the caller's device buffers and keeps its own
+scratch in a static device array.  Here it is called through the C ABI
+twice in a row, on different inputs, and each result is compared with
+mpm_compgraph_mass_loss (CompGraph.end_layer_mass_loss) on the same
+particles: loss within 1e-6 relative, dL/dx within 1e-5 in norm (both FP32;
+only the order of the atomic sums differs).  A call after the first one
+leaves the device's free memory unchanged, and a stream under capture is
+refused (the call is synchronous).
 """
 import ctypes as C
 
@@ -65,6 +67,64 @@ def test_noalloc_mass_loss_matches_regular_entry_point(dm, adjoint):
         assert abs(loss - want_loss) <= 1e-6 * abs(want_loss), (call, loss, want_loss)
         err = np.linalg.norm(gx - want_gx) / np.linalg.norm(want_gx)
         assert err <= 1e-5, (call, err)
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged(dm):
+    """After one call on the device (which loads the library's module and so
+    its static scratch), a further call on other inputs changes the device's
+    free memory by nothing: no allocation happens on the call path."""
+    torch = pytest.importorskip("torch")
+    a, b = _inputs(1, 0.0), _inputs(2, 0.011)
+    _noalloc(dm, torch, *a, False)  # module load happens here, if not before
+    dev = torch.device("cuda")
+    w, g, tgt = b
+    x = torch.tensor(w.x, dtype=torch.float32, device=dev).contiguous()
+    m = torch.tensor(w.m, dtype=torch.float32, device=dev).contiguous()
+    t = torch.tensor(tgt, dtype=torch.float32, device=dev).contiguous()
+    gx = torch.empty((w.n, 3), dtype=torch.float32, device=dev)
+    dims = (C.c_int * 3)(*g.dims)
+    mn = (C.c_double * 3)(*g.min)
+    loss = C.c_double()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = dm._lib.lib.mpm_mass_loss_noalloc(w.n, C.c_void_p(x.data_ptr()), C.c_void_p(m.data_ptr()),
+                                          C.c_void_p(t.data_ptr()), dims, C.c_double(g.dx), mn, 1,
+                                          C.c_void_p(gx.data_ptr()), C.byref(loss), None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert rc == 0, dm._lib.lib.mpm_last_error()
+    assert free1 == free0, (free0, free1)
+    assert np.isfinite(loss.value) and torch.isfinite(gx).all()
+
+
+def test_noalloc_refuses_a_stream_under_capture(dm):
+    """The call is synchronous, so a stream being captured is refused before
+    any work is queued on it; the capture itself stays valid."""
+    torch = pytest.importorskip("torch")
+    w, g, tgt = _inputs(3, 0.0)
+    dev = torch.device("cuda")
+    x = torch.tensor(w.x, dtype=torch.float32, device=dev).contiguous()
+    m = torch.tensor(w.m, dtype=torch.float32, device=dev).contiguous()
+    t = torch.tensor(tgt, dtype=torch.float32, device=dev).contiguous()
+    gx = torch.zeros((w.n, 3), dtype=torch.float32, device=dev)
+    dims = (C.c_int * 3)(*g.dims)
+    mn = (C.c_double * 3)(*g.min)
+    loss = C.c_double()
+    y = torch.zeros(4, device=dev)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        rc = dm._lib.lib.mpm_mass_loss_noalloc(w.n, C.c_void_p(x.data_ptr()), C.c_void_p(m.data_ptr()),
+                                              C.c_void_p(t.data_ptr()), dims, C.c_double(g.dx), mn, 0,
+                                              C.c_void_p(gx.data_ptr()), C.byref(loss),
+                                              C.c_void_p(side.cuda_stream))
+        y.add_(1.0)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert rc == dm._lib.MPM_ERR_STATE
+    assert b"captured" in dm._lib.lib.mpm_last_error()
+    assert float(y.sum()) == 4.0
 
 
 def test_noalloc_rejects_oversized_grid(dm):
