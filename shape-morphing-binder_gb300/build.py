@@ -15,7 +15,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 INCLUDE = HERE.parent / "include"
 LIB = HERE / "diffmpm_bindings" / "libmpm.so"
-SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu", "mpm_geometry.cu", "gs_rasterizer.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_engine.cu", "mpm_noalloc.cu", "mpm_sort.cu", "mpm_geometry.cu", "mpm_checks.cu",
+           "gs_rasterizer.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

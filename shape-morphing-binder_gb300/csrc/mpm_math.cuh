@@ -410,10 +410,19 @@ MPM_HD bool polar_newton(const R* F, R* Rm)
     return true;
 }
 
+// Branch flags some device functions can report (a null flag pointer, the
+// default, compiles the reporting away): which guarded or clamped form ran.
+enum {
+    BR_POLAR_SVD = 1,      // polar decomposition by the FP64 SVD (FP32 Newton not used)
+    BR_INV_FP64 = 2,       // det F and F^{-T} formed in FP64 (J <= 0.25)
+    BR_J_CLAMP = 4,        // J clamped at 1e-6 (Elasticity.cpp:52)
+    BR_DR_REGULARISED = 8  // rotation-derivative solve regularised (det A < 1e-6, Elasticity.cpp:57-117)
+};
+
 // F = R S.  The FP32 path uses Newton when F is safely away from inversion
 // and the FP64 SVD otherwise (the FP64 guard).
 template <typename R>
-MPM_HD void polar(const R* F, R* Rm, R* S)
+MPM_HD void polar(const R* F, R* Rm, R* S, unsigned* fl = nullptr)
 {
     R J = det3(F);
     R n2 = dot9(F, F);
@@ -424,6 +433,7 @@ MPM_HD void polar(const R* F, R* Rm, R* S)
         for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
         polar_svd(Fd, Rd);
         for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+        if (fl) *fl |= BR_POLAR_SVD;
     }
     R RtF[9];
     mulTN3(Rm, F, RtF);
@@ -447,7 +457,7 @@ struct Inv {
 };
 
 template <typename R>
-MPM_HD void invariants(const R* F, Inv<R>& v)
+MPM_HD void invariants(const R* F, Inv<R>& v, unsigned* fl = nullptr)
 {
     R jm1 = det_minus_one(F);
     R J = R(1) + jm1;
@@ -470,15 +480,16 @@ MPM_HD void invariants(const R* F, Inv<R>& v)
         v.Jraw = (R)Jd;
         v.Jc = (R)Jcd;
         v.Jm1c = (R)(Jcd - 1.0);
+        if (fl) *fl |= BR_INV_FP64 | (Jd > 1e-6 ? 0u : (unsigned)BR_J_CLAMP);
     }
 }
 
 // P(F): FCR (Elasticity.cpp:45-55) or Neo-Hookean.  R/S are returned for reuse.
 template <typename R>
-MPM_HD void pk(int material, const R* F, R lam, R mu, const Inv<R>& iv, R* P, R* Rm, R* S)
+MPM_HD void pk(int material, const R* F, R lam, R mu, const Inv<R>& iv, R* P, R* Rm, R* S, unsigned* fl = nullptr)
 {
     if (material == MAT_FCR) {
-        polar(F, Rm, S);
+        polar(F, Rm, S, fl);
         R k = lam * iv.Jm1c * iv.Jc;
 #pragma unroll
         for (int i = 0; i < 9; ++i) P[i] = R(2) * mu * (F[i] - Rm[i]) + k * iv.Fit[i];
@@ -489,12 +500,38 @@ MPM_HD void pk(int material, const R* F, R lam, R mu, const Inv<R>& iv, R* P, R*
     }
 }
 
+// Derivative of the polar rotation applied to G: with A = tr(S) I - S,
+// A w = axial(R^T G - G^T R) and dR = R [w]x, regularising A by 1e-4 on the
+// diagonal when det A < 1e-6 (Elasticity.cpp:57-117).
+template <typename T>
+MPM_HD void rotation_vjp(const T* Rm, const T* S, const T* G, T* dR, unsigned* fl)
+{
+    T A[9] = {S[4] + S[8], -S[1], -S[2], -S[1], S[0] + S[8], -S[5], -S[2], -S[5], S[0] + S[4]};
+    if (fabs(det3(A)) < T(1e-6)) {
+        A[0] += T(1e-4);
+        A[4] += T(1e-4);
+        A[8] += T(1e-4);
+        if (fl) *fl |= BR_DR_REGULARISED;
+    }
+    T rg[9];
+    mulTN3(Rm, G, rg);
+    const T b3[3] = {rg[7] - rg[5], rg[2] - rg[6], rg[3] - rg[1]};
+    T c[9];
+    cof3(A, c);
+    const T idet = rcp(A[0] * c[0] + A[1] * c[1] + A[2] * c[2]);
+    const T w0 = (c[0] * b3[0] + c[3] * b3[1] + c[6] * b3[2]) * idet;
+    const T w1 = (c[1] * b3[0] + c[4] * b3[1] + c[7] * b3[2]) * idet;
+    const T w2 = (c[2] * b3[0] + c[5] * b3[1] + c[8] * b3[2]) * idet;
+    const T W[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
+    mul3(Rm, W, dR);
+}
+
 // VJP of P(F) applied to G = dL/dP; returns dL/dF.  exact == false follows
 // d2_FCE_psi_dF2_mult_by_dF (Elasticity.cpp:57-117), including its use of
 // the clamped J next to the unclamped one inside d(J F^{-T})/dF.
 template <typename R>
 MPM_HD void pk_vjp(int material, bool exact, const R* F, R lam, R mu, const Inv<R>& iv, const R* Rm, const R* S,
-                   const R* G, R* out)
+                   const R* G, R* out, unsigned* fl = nullptr)
 {
     const R* Fit = iv.Fit;
     R fg = dot9(Fit, G);
@@ -513,24 +550,27 @@ MPM_HD void pk_vjp(int material, bool exact, const R* F, R lam, R mu, const Inv<
             for (int i = 0; i < 9; ++i) out[i] = R(2) * mu * G[i] - b * sw[i];
         }
         // -2 mu dR: (tr S I - S) w = axial(R^T G - G^T R), dR = R [w]x
-        R A[9] = {S[4] + S[8], -S[1], -S[2], -S[1], S[0] + S[8], -S[5], -S[2], -S[5], S[0] + S[4]};
-        if (fabs(det3(A)) < R(1e-6)) {
-            A[0] += R(1e-4);
-            A[4] += R(1e-4);
-            A[8] += R(1e-4);
-        }
-        R rg[9];
-        mulTN3(Rm, G, rg);
-        R b3[3] = {rg[7] - rg[5], rg[2] - rg[6], rg[3] - rg[1]};
-        R c[9];
-        cof3(A, c);
-        R idet = rcp(A[0] * c[0] + A[1] * c[1] + A[2] * c[2]);
-        R w0 = (c[0] * b3[0] + c[3] * b3[1] + c[6] * b3[2]) * idet;
-        R w1 = (c[1] * b3[0] + c[4] * b3[1] + c[7] * b3[2]) * idet;
-        R w2 = (c[2] * b3[0] + c[5] * b3[1] + c[8] * b3[2]) * idet;
-        R W[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
+        const R A[9] = {S[4] + S[8], -S[1], -S[2], -S[1], S[0] + S[8], -S[5], -S[2], -S[5], S[0] + S[4]};
         R dR[9];
-        mul3(Rm, W, dR);
+        if (sizeof(R) == 4 && fabs(det3(A)) < R(1e-6)) {
+            // FP64 guard: A near singular (two signed singular values of F
+            // nearly cancel, which only an inverted or near-singular F
+            // reaches) makes the solve ill-conditioned, beyond what FP32
+            // holds -- redo R, S and the regularised solve in FP64 from F
+            double Fd[9], Rd[9], Gd[9], RtF[9], Sd[9], dRd[9];
+            for (int i = 0; i < 9; ++i) {
+                Fd[i] = (double)F[i];
+                Gd[i] = (double)G[i];
+            }
+            polar_svd(Fd, Rd);
+            mulTN3(Rd, Fd, RtF);
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) Sd[r * 3 + c] = 0.5 * (RtF[r * 3 + c] + RtF[c * 3 + r]);
+            rotation_vjp(Rd, Sd, Gd, dRd, fl);
+            for (int i = 0; i < 9; ++i) dR[i] = (R)dRd[i];
+        } else {
+            rotation_vjp(Rm, S, G, dR, fl);
+        }
 #pragma unroll
         for (int i = 0; i < 9; ++i) out[i] -= R(2) * mu * dR[i];
     } else {

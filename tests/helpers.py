@@ -109,3 +109,48 @@ def golden_opt_case(go):
     kw = {k: (float(go[k]) if k in ("initial_alpha", "gd_tol") else int(go[k]))
           for k in ("num_steps", "control_stride", "max_gd_iters", "max_ls_iters", "initial_alpha", "gd_tol")}
     return s, g, go["target"], prm, kw
+
+
+def compressive_case(seed=0, G=16, k=150.0):
+    """A rollout start in the regime where the guarded and clamped branches
+    switch in.  Particles of a sphere (rho 60) move with v = -k (x - c), so
+    the first G2P gives tr C ~ -3k (-450: det(I + dt C) ~ 0.61 at dt 1e-3,
+    which trips the J trust region, ForwardSimulation.cpp:135-152).  F0
+    comes in four families: near identity; uniformly compressed (J ~ 0.17:
+    FP64 invariants, and J0 < kJmin makes the trust scale 0); near-singular
+    anisotropic (F ~ diag(1.6, 1, 0.01): the FP64 SVD polar decomposition);
+    inverted (F ~ diag(1, 1, -0.2): J clamped at 1e-6, Elasticity.cpp:52).
+    Returns (state, grid, rng, family index per particle)."""
+    import oracle as O
+    from diffmpm_bindings import workloads as W
+    w = W.sphere32(seed=seed, G=G, rho=60.0)
+    rng = np.random.default_rng(seed)
+    n = w.n
+    v = -k * (w.x - np.array([0.5, 0.5, 0.5]))
+    F = np.tile(np.eye(3), (n, 1, 1)) + 0.02 * rng.normal(size=(n, 3, 3))
+    fam = rng.integers(0, 4, size=n)
+    F[fam == 1] = 0.55 * np.eye(3) + 0.01 * rng.normal(size=((fam == 1).sum(), 3, 3))
+    F[fam == 2] = np.diag([1.6, 1.0, 0.01]) + 0.005 * rng.normal(size=((fam == 2).sum(), 3, 3))
+    F[fam == 3] = np.diag([1.0, 1.0, -0.2]) + 0.01 * rng.normal(size=((fam == 3).sum(), 3, 3))
+    s0 = O.State(w.x, v, np.zeros((n, 3, 3)), F, w.m, w.vol, w.lam, w.mu, 0.01 * rng.normal(size=(n, 3, 3)))
+    return s0, O.Grid(w.dims, w.dx), rng, fam
+
+
+def oracle_branch_counts(orc, grid, prm, s0, T):
+    """Per forward step of the oracle rollout: particles whose F + dFc takes
+    the FP64 invariants (J <= 0.25), the J clamp (J <= 1e-6), the FP64 SVD
+    guard (J <= 0.05 (|F|/sqrt 3)^3), and whose C was rescaled by the trust
+    region (0 < s < 1) or zeroed by it (s <= 0)."""
+    out = []
+    s = s0
+    for _ in range(T):
+        Ft = s.F + (s.dFc if s.dFc is not None else 0.0)
+        J = np.linalg.det(Ft)
+        nrm = np.sqrt((Ft ** 2).sum(axis=(1, 2)))
+        s1, st = orc.forward_step(grid, prm, s)
+        tr = st["trust"]
+        out.append(dict(inv64=int((J <= 0.25).sum()), jclamp=int((J <= 1e-6).sum()),
+                        svd=int((J <= 0.05 * (nrm / np.sqrt(3)) ** 3).sum()),
+                        rescaled=int(((tr > 0) & (tr < 1)).sum()), zeroed=int((tr <= 0).sum())))
+        s = s1
+    return out

@@ -54,3 +54,27 @@ def test_reference_adjoint_differs_from_fd(orc):
     fd = _fd(orc, g, prm, s0, T, seed_gx, "dFc", d, 1e-5)
     an = float((gr.F * d).sum())
     assert abs(an - fd) > 1e-3 * abs(fd)
+
+
+def test_exact_adjoint_matches_fd_under_compression(orc):
+    """The compressive case (tests/helpers.compressive_case): the trust region
+    rescales or zeroes C, F0 includes inverted, near-singular and strongly
+    compressed matrices (J clamp, FP64-guard regime).  The exact adjoint is
+    still the derivative of the forward pass."""
+    from helpers import compressive_case, oracle_branch_counts
+    s0, g, rng, _ = compressive_case(seed=1)
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.1, exact=True)
+    T = 4
+    counts = oracle_branch_counts(orc, g, prm, s0, T)
+    assert all(min(c.values()) > 0 for c in counts), counts
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    _, gr = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    grads = dict(v=gr.v, x=gr.x, F=gr.F, dFc=gr.Ft)
+    # eps 1e-6 (1e-7 for x): smaller steps lose the difference to rounding in
+    # this violent case, larger ones straddle the clamps' kinks
+    for field, eps in (("v", 1e-6), ("dFc", 1e-6), ("F", 1e-6), ("x", 1e-7)):
+        for _ in range(3):
+            d = rng.normal(size=grads[field].shape)
+            fd = _fd(orc, g, prm, s0, T, seed_gx, field, d, eps)
+            an = float((grads[field] * d).sum())
+            assert abs(an - fd) <= 1e-5 * abs(fd), (field, an, fd)
