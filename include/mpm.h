@@ -220,12 +220,22 @@ int mpm_compgraph_adam_step(mpm_compgraph* cg, int layer, double alpha, double g
 /* OptimizeSingleTimestep (CompGraph.cpp:369-465; bind.cpp:294-317) */
 int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int timestep_idx, int max_gd_iters,
                                            int current_episode, double initial_alpha, int max_line_search_iters);
+/* No counterpart in the reference, where OptimizeSingleTimestep's Adam step
+ * counter is a function-local static shared by every CompGraph of the
+ * process (CompGraph.cpp:396) that no caller can read or reset; this library
+ * keeps the same process-wide counter.  *get (if get) receives it, then
+ * *set (if set, >= 0) replaces it -- e.g. 0 to start a sequence of calls as
+ * a fresh reference process would. */
+int mpm_single_timestep_adam_step(int* get, const int* set);
 /* OptimizeDefGradControlSequence (CompGraph.cpp:213-368; bind.cpp:165-172) */
 int mpm_compgraph_run_optimization(mpm_compgraph* cg, const mpm_opt_input* opt);
 /* No counterpart in the reference (which prints them): every loss the last
  * run_optimization evaluated, in order -- the initial loss, per gradient
  * step the loss before the step and each line-search trial, and the final
- * loss.  *count receives the total; at most cap values are copied. */
+ * loss -- or, after optimize_single_timestep, the losses that call
+ * evaluated (per gradient step the loss before the step and each
+ * line-search trial).  *count receives the total; at most cap values are
+ * copied. */
 int mpm_compgraph_loss_history(const mpm_compgraph* cg, double* out, int cap, int* count);
 /* forward and adjoint particle steps executed since load (recomputed
  * forward steps of checkpointed backward passes count as forward steps) */
@@ -239,6 +249,25 @@ int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long*
 int mpm_compgraph_nonfinite(mpm_compgraph* cg, int layer, int grads, int* flag);
 /* number of grid nodes with mass > 0 in the forward grid of `layer` (the
  * last forward step's grid when the graph is checkpointed) -- see above */
+
+/* PK_FixedCorotatedElasticity (Elasticity.cpp:45-55) and
+ * d2_FCE_psi_dF2_mult_by_dF (Elasticity.cpp:57-117; the reference's only
+ * callers are P_op_1 and Back_Timestep, ForwardSimulation.cpp:16-24,
+ * BackPropagation.cpp:76-143), evaluated by the engine's own device code --
+ * the functions P2G and its transpose inline -- on n matrices, so that the
+ * branches a rollout rarely reaches can be checked: the FP64 guard near
+ * inversion, the J clamp and the regularised rotation derivative.  precision
+ * MPM_FP32 (FP32 with the FP64 guard; inputs rounded to float) or MPM_FP64;
+ * material MPM_MAT_*; adjoint MPM_ADJ_REFERENCE (the reference's derivative)
+ * or MPM_ADJ_EXACT.  Host arrays, double, row-major: F and G (n,3,3), lam
+ * and mu (n); out: P (n,3,3) the stress, dP (n,3,3) the derivative of P at F
+ * applied to G (the Hessian is symmetric, so this is also the VJP the
+ * adjoint uses), branches (n ints, may be NULL): bit 0 FP64 SVD polar
+ * decomposition, bit 1 FP64 det F / F^-T, bit 2 J clamped at 1e-6, bit 3
+ * regularised rotation-derivative solve.  Synchronous; allocates its
+ * device buffers. */
+int mpm_constitutive(int n, int precision, int material, int adjoint, const double* F, const double* G,
+                     const double* lam, const double* mu, double* P, double* dP, int* branches);
 
 /* ---------------------------------------------------------- measurement */
 /* kernel ids for the profiler */

@@ -345,6 +345,111 @@ class Oracle:
         return np.array(hist), layers
 
 
+class OracleGraph:
+    """CompGraph's layer tape, loss, backward with render gradients and
+    OptimizeSingleTimestep (CompGraph.cpp:21-211, 369-465) over the FP64
+    step, loss and Adam of ``Oracle``.  Test infrastructure: the checker for
+    the engine's optimize_single_timestep.
+
+    As in the reference: SetUpCompGraph copies layer 0 into every layer
+    (CompGraph.cpp:30-40), so each layer has its own zero Adam moments; a
+    forward pass from layer t rewrites layers t+1.. and zeroes their control
+    (ForwardSimulation.cpp:155); EndLayerMassLoss sets the last layer's dL/dx
+    and zeroes its other gradients; ComputeBackwardPass first adds the stored
+    render gradients to the last layer (CompGraph.cpp:148-197); the control
+    gradient is dL/dF of the control layer, or dL/d(F + dFc) for the exact
+    adjoint.  OptimizeSingleTimestep's Adam step counter is a function-local
+    static in the reference (CompGraph.cpp:396), shared by every graph of the
+    process: here it is the class attribute ``adam_step``."""
+
+    adam_step = 0
+
+    def __init__(self, orc: "Oracle", grid: Grid, prm: Params, s0: State, target_m):
+        self.orc, self.grid, self.prm = orc, grid, prm
+        n = s0.n
+        self.target = _f64(target_m)
+        first = State(s0.x, s0.v, s0.C, s0.F, s0.m, s0.vol, s0.lam, s0.mu,
+                      s0.dFc if s0.dFc is not None else np.zeros((n, 3, 3)))
+        self.layers = [first]
+        self.steps = []
+        self.moments = {}
+        self.render = None
+        self.history = []
+
+    @property
+    def n(self) -> int:
+        return self.layers[0].n
+
+    def set_up(self, num_layers: int):
+        import copy
+        self.layers = [self.layers[0]] + [copy.deepcopy(self.layers[0]) for _ in range(num_layers - 1)]
+        self.steps = [None] * (num_layers - 1)
+
+    def set_render_gradients(self, dLdF, dLdx):
+        n = self.n
+        self.render = (_f64(dLdF, (n, 3, 3)), _f64(dLdx, (n, 3)))
+
+    def forward(self, start: int):
+        for i in range(start, len(self.layers) - 1):
+            nxt, st = self.orc.forward_step(self.grid, self.prm, self.layers[i])
+            nxt.dFc = np.zeros((self.n, 3, 3))
+            self.layers[i + 1], self.steps[i] = nxt, st
+
+    def loss(self):
+        last = self.layers[-1]
+        loss, aux = self.orc.mass_loss(self.grid, self.prm, last.x, last.m, self.target)
+        self.last_gx = aux["gx"]
+        self.history.append(loss)
+        return loss
+
+    def backward(self, ctl: int):
+        n = self.n
+        gx = np.array(self.last_gx, np.float64)
+        gF = np.zeros((n, 3, 3))
+        if self.render is not None:
+            gF = gF + self.render[0]
+            gx = gx + self.render[1]
+        g = Grads(gx, np.zeros((n, 3)), gF, np.zeros((n, 3, 3)))
+        for t in range(len(self.layers) - 2, ctl - 1, -1):
+            g = self.orc.backward_step(self.grid, self.prm, self.layers[t], self.layers[t + 1].C, self.steps[t], g,
+                                       want_ft=(t == ctl))
+        return g.Ft if self.prm.exact else g.F
+
+    def optimize_single_timestep(self, t: int, max_gd_iters: int = 1, episode: int = 0, initial_alpha: float = 1.0,
+                                 max_ls_iters: int = 10):
+        """OptimizeSingleTimestep (CompGraph.cpp:369-465); the losses it
+        evaluates are appended to ``history``."""
+        if t < 0 or t >= len(self.layers) - 1:
+            return
+        alpha = initial_alpha
+        lay = self.layers[t]
+        for _ in range(max_gd_iters):
+            self.forward(t)
+            loss = self.loss()
+            if not np.isfinite(loss):
+                break
+            gc = self.backward(t)
+            gn = max(self.orc.grad_norm(gc), 1e-12)
+            mom = self.moments.setdefault(t, [np.zeros((self.n, 3, 3)) for _ in range(3)])
+            bak = [lay.dFc.copy()] + [a.copy() for a in mom]
+            ok, a = False, alpha
+            for _ls in range(max_ls_iters):
+                self.orc.adam(gc, lay.dFc, mom[0], mom[1], mom[2], a, gn, timestep=OracleGraph.adam_step + 1)
+                self.forward(t)
+                nl = self.loss()
+                if np.isfinite(nl) and nl < loss:
+                    OracleGraph.adam_step += 1
+                    alpha = min(a * 1.1, initial_alpha)
+                    ok = True
+                    break
+                lay.dFc[...] = bak[0]
+                for dst, src in zip(mom, bak[1:]):
+                    dst[...] = src
+                a *= 0.5
+            if not ok:
+                break
+
+
 class Reference:
     """The reference's own DiffMPMLib3D compiled from source (float or double)."""
 
@@ -462,6 +567,36 @@ class Reference:
                                      C.c_int(max_ls_iters), C.c_double(initial_alpha), C.c_double(gd_tol),
                                      _p(dfc), _p(xT), log, C.c_int(len(log)))
         return loss, dfc, xT, log.value.decode(errors="replace")
+
+    def optimize_single(self, grid: Grid, prm: Params, s: State, target_m, num_layers: int, calls,
+                        render_dLdF=None, render_dLdx=None):
+        """run.py's E2E sequence (set_up_comp_graph, compute_forward_pass(0),
+        optional set_render_gradients, then OptimizeSingleTimestep per call
+        (t, max_gd, alpha, max_ls)) on the reference: per call, every layer's
+        dFc (calls, L, N, 3, 3), the last positions (calls, N, 3) and
+        EndLayerMassLoss, and the printed lines.  The reference's Adam step
+        counter for this call is process-wide: call this once per process."""
+        dims, dx, mn = self._g(grid)
+        n, k = s.n, len(calls)
+        t = (C.c_int * k)(*[int(c[0]) for c in calls])
+        gd = (C.c_int * k)(*[int(c[1]) for c in calls])
+        al = (C.c_double * k)(*[float(c[2]) for c in calls])
+        ls = (C.c_int * k)(*[int(c[3]) for c in calls])
+        dfc = np.zeros((k, num_layers, n, 3, 3))
+        xT = np.zeros((k, n, 3))
+        loss = np.zeros(k)
+        log = C.create_string_buffer(1 << 16)
+        fp = C.POINTER(C.c_float)
+        rF = None if render_dLdF is None else np.ascontiguousarray(render_dLdF, np.float32).reshape(n, 9)
+        rx = None if render_dLdx is None else np.ascontiguousarray(render_dLdx, np.float32).reshape(n, 3)
+        rc = self.lib.ref_optimize_single(dims, dx, _p(mn), C.c_double(prm.dt), C.c_double(prm.drag),
+                                          C.c_double(prm.smoothing), C.c_int(n), _p(s.x), _p(s.v), _p(s.F),
+                                          _p(s.m), _p(s.vol), _p(s.lam), _p(s.mu), _p(_f64(target_m)),
+                                          C.c_int(num_layers), None if rF is None else rF.ctypes.data_as(fp),
+                                          None if rx is None else rx.ctypes.data_as(fp), C.c_int(k), t, gd, al, ls,
+                                          _p(dfc), _p(xT), _p(loss), log, C.c_int(len(log)))
+        assert rc == 0
+        return dfc, xT, loss, log.value.decode(errors="replace")
 
     def sample_mesh(self, V, F, dx: float):
         """GeneratePointCloudFromWatertightTriangleMesh over the mesh's bounding

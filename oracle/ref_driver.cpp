@@ -314,6 +314,60 @@ double ref_optimize(const int* dims, double dx, const double* mn, double dt, dou
     return loss;
 }
 
+// The E2E path of run.py (run.py:1146-1149,665,686) on a graph built from
+// arrays: SetUpCompGraph(num_layers), ComputeForwardPass(0, 0), optional
+// render gradients (the members set_render_gradients fills, bind.cpp:359-451),
+// then `calls` OptimizeSingleTimestep calls (CompGraph.cpp:369-465), call c
+// with (t[c], max_gd[c], episode 0, alpha[c], max_ls[c]).  After each call it
+// records every layer's dFc (dFc_out: (calls, L, N, 3, 3)), the last layer's
+// positions (xT: (calls, N, 3)) and EndLayerMassLoss (loss: (calls)).  The
+// optimiser's own lines go to `log` (cap bytes).  OptimizeSingleTimestep's
+// Adam step counter is a function-local static (CompGraph.cpp:396): it
+// starts at 0 in a fresh process and carries over between calls.
+int ref_optimize_single(const int* dims, double dx, const double* mn, double dt, double drag, double smoothing,
+                        int n, const double* x0, const double* v0, const double* F0, const double* m,
+                        const double* vol, const double* lam, const double* mu, const double* target_m,
+                        int num_layers, const float* render_dLdF, const float* render_dLdx, int calls,
+                        const int* t, const int* max_gd, const double* alpha, const int* max_ls, double* dFc_out,
+                        double* xT, double* loss, char* log, int cap)
+{
+    auto pc = make_pc(n, x0, v0, nullptr, F0, nullptr, m, vol, lam, mu);
+    auto grid = make_grid(dims, dx, mn);
+    auto tgt = make_grid(dims, dx, mn);
+    for (size_t i = 0; i < tgt->nodes.size(); ++i) tgt->nodes[i].m = (Real)target_m[i];
+    std::ostringstream text;
+    std::streambuf* old = std::cout.rdbuf(text.rdbuf());
+    CompGraph cg(pc, grid, tgt);
+    cg.dt = (Real)dt;
+    cg.drag = (Real)drag;
+    cg.smoothing_factor = (Real)smoothing;
+    cg.SetUpCompGraph(num_layers);
+    cg.ComputeForwardPass(0, 0);
+    if (render_dLdF && render_dLdx) {
+        cg.stored_render_grad_F_.assign(render_dLdF, render_dLdF + 9 * (size_t)n);
+        cg.stored_render_grad_x_.assign(render_dLdx, render_dLdx + 3 * (size_t)n);
+        cg.render_grad_num_points_ = (size_t)n;
+        cg.has_render_grads_ = true;
+    }
+    const size_t L = cg.layers.size();
+    for (int c = 0; c < calls; ++c) {
+        cg.OptimizeSingleTimestep(t[c], max_gd[c], 0, (Real)alpha[c], max_ls[c]);
+        for (size_t l = 0; l < L; ++l)
+            for (int p = 0; p < n; ++p)
+                put(cg.layers[l].point_cloud->points[p].dFc, dFc_out + (((size_t)c * L + l) * n + p) * 9);
+        for (int p = 0; p < n; ++p) put(cg.layers.back().point_cloud->points[p].x, xT + ((size_t)c * n + p) * 3);
+        loss[c] = cg.EndLayerMassLoss();
+    }
+    std::cout.rdbuf(old);
+    if (log && cap > 0) {
+        const std::string s = text.str();
+        const size_t k = std::min(s.size(), (size_t)cap - 1);
+        memcpy(log, s.data(), k);
+        log[k] = 0;
+    }
+    return 0;
+}
+
 // GeneratePointCloudFromWatertightTriangleMesh (GeometryLoading.cpp:10-83)
 // over the mesh's bounding box, as LoadMPMPointCloudFromObj calls it
 // (GeometryLoading.cpp:103-118): writes up to cap points (cap,3) and returns

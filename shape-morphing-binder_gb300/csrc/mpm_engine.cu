@@ -576,7 +576,7 @@ struct Graph {
     std::vector<InstHost> inst;
     Buf inst_table;
     long long total_nodes = 0;
-    std::vector<double> loss_hist;  // losses evaluated by the last run_optimization
+    std::vector<double> loss_hist;  // losses evaluated by the last run_optimization / optimize_single
     bool resort_on = true;           // re-sort the particles by cell at set-up
     // render gradients (stored on the host like CompGraph.h:73-76)
     std::vector<float> rgF, rgx;
@@ -1317,9 +1317,11 @@ void graph_optimize_single(Graph& G, int t, int max_gd, int episode, double alph
     const double beta1 = 0.9, beta2 = 0.999, eps = 1e-3;
     double alpha = alpha0;
     Backup bk;
+    G.loss_hist.clear();
     for (int it = 0; it < max_gd; ++it) {
         graph_forward<R>(G, t);
         double loss = graph_loss<R>(G);
+        G.loss_hist.push_back(loss);
         if (!std::isfinite(loss)) {
             say("Warning: Non-finite loss. Aborting.\n");
             break;
@@ -1334,6 +1336,7 @@ void graph_optimize_single(Graph& G, int t, int max_gd, int episode, double alph
             graph_adam<R>(G, t, a, gn, beta1, beta2, eps, g_single_step_adam_t + 1);
             graph_forward<R>(G, t);
             double nl = graph_loss<R>(G);
+            G.loss_hist.push_back(nl);
             if (std::isfinite(nl) && nl < loss) {
                 ++g_single_step_adam_t;
                 alpha = std::min(a * 1.1, alpha0);
@@ -2028,6 +2031,17 @@ int mpm_compgraph_optimize_single_timestep(mpm_compgraph* cg, int t, int max_gd,
         with_prec(cg->g.prec, [&](auto r) { graph_optimize_single<decltype(r)>(cg->g, t, max_gd, episode, alpha, max_ls); });
         ck(cudaStreamSynchronize(cg->g.stream), "optimize");
         check_fix(cg->g, false);
+    });
+}
+
+int mpm_single_timestep_adam_step(int* get, const int* set)
+{
+    return guard([&] {
+        if (get) *get = g_single_step_adam_t;
+        if (set) {
+            if (*set < 0) fail(MPM_ERR_ARG, "the Adam step count is non-negative");
+            g_single_step_adam_t = *set;
+        }
     });
 }
 

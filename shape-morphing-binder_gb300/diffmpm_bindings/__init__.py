@@ -464,7 +464,8 @@ class CompGraph:
         check(lib.mpm_compgraph_run_optimization(self._h, C.byref(o)), "run_optimization")
 
     def loss_history(self) -> np.ndarray:
-        """Every loss the last run_optimization evaluated, in order (additive)."""
+        """Every loss the last run_optimization or optimize_single_timestep
+        evaluated, in order (additive)."""
         n = C.c_int()
         check(lib.mpm_compgraph_loss_history(self._h, None, 0, C.byref(n)))
         out = np.zeros(n.value)
@@ -652,6 +653,16 @@ def load_point_cloud_from_obj(obj_path: str, opt: OptInput, precision=None) -> P
     return PointCloud.from_arrays(pts.astype(np.float32), m=np.full(n, m, np.float32),
                                   vol=np.full(n, vol, np.float32), lam=np.full(n, opt.lam, np.float32),
                                   mu=np.full(n, opt.mu, np.float32), precision=precision)
+
+
+def single_timestep_adam_step(set_to=None) -> int:
+    """OptimizeSingleTimestep's process-wide Adam step counter (a
+    function-local static in the reference, CompGraph.cpp:396): returns it
+    and, with ``set_to``, replaces it afterwards (additive)."""
+    cur = C.c_int()
+    new = None if set_to is None else C.byref(C.c_int(int(set_to)))
+    check(lib.mpm_single_timestep_adam_step(C.byref(cur), new), "single_timestep_adam_step")
+    return cur.value
 
 
 def step_count():

@@ -12,7 +12,8 @@ import ctypes as C
 import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libmpm.so"
+# the in-tree build; MPM_LIB_PATH names another build of the same library
+LIB_PATH = Path(os.environ.get("MPM_LIB_PATH") or Path(__file__).resolve().parent / "libmpm.so")
 
 MPM_OK, MPM_ERR_ARG, MPM_ERR_SHAPE, MPM_ERR_OOM, MPM_ERR_NONFINITE, MPM_ERR_TIMEOUT, MPM_ERR_CUDA, \
     MPM_ERR_STATE, MPM_ERR_RANGE = range(9)
@@ -125,6 +126,8 @@ _SIGS = {
     "mpm_kernel_name": [C.c_int],
     "mpm_launch_count": [],
     "mpm_mass_loss_noalloc": [C.c_int, _vp, _vp, _vp, _ip, C.c_double, _dp, C.c_int, _vp, _dp, _vp],
+    "mpm_constitutive": [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip],
+    "mpm_single_timestep_adam_step": [_ip, _ip],
 }
 _RESTYPE = {"mpm_last_error": C.c_char_p, "mpm_kernel_name": C.c_char_p, "mpm_launch_count": C.c_longlong, "mpm_default_params": None, "mpm_default_options": None,
             "mpm_set_verbose": None, "mpm_step_count": None}

@@ -6,13 +6,14 @@ the reference's ForwardTimeStep, Back_Timestep, EndLayerMassLoss,
 Descend_Adam, CalculatePointCloudVolumes, PK_FixedCorotatedElasticity and
 d2_FCE_psi_dF2_mult_by_dF, plus a 5-step full-tape forward/backward through
 CompGraph (reference_small.npz), and a run of the control-sequence
-optimiser OptimizeDefGradControlSequence (reference_optimize.npz) and the
+optimiser OptimizeDefGradControlSequence (reference_optimize.npz), the
 mesh -> lattice sampler GeneratePointCloudFromWatertightTriangleMesh on two
-procedural meshes (reference_mesh_sampling.npz).  The
+procedural meshes (reference_mesh_sampling.npz), and run.py's E2E sequence of
+OptimizeSingleTimestep calls with render gradients (reference_single.npz).  The
 fixtures travel with the repository; the GPU tests compare against them
 without the reference present.
 
-Usage: python tests/golden/make_golden.py [--only small|optimize|mesh]
+Usage: REF_DIR=<reference checkout> python tests/golden/make_golden.py [--only small|optimize|mesh|single]
 """
 from __future__ import annotations
 
@@ -129,7 +130,59 @@ def make_optimize():
     print("wrote", OUT / "reference_optimize.npz", "N =", s.n)
 
 
-def main(which=("small", "optimize", "mesh")):
+# run.py's E2E physics path: layers, then OptimizeSingleTimestep calls
+# (t, max_gd_iters, initial_alpha, max_line_search_iters), with render
+# gradients stored on the graph
+SINGLE_CALLS = [(2, 2, 0.05, 4), (0, 2, 0.05, 4), (2, 1, 0.05, 4), (4, 2, 0.5, 3)]
+SINGLE_LAYERS = 6
+
+
+def single_case():
+    """Inputs of the single-timestep fixture: the optimiser fixture's
+    particles and target, dt 2e-3, drag 0.5, smoothing 0.1, seeded render
+    gradients dL/dF (N,3,3) and dL/dx (N,3) (float32, as run.py passes them)."""
+    w, s, g, tgt, _ = optimize_case()
+    prm = O.Params(dt=2e-3, drag=0.5, smoothing=0.1)
+    rng = np.random.default_rng(17)
+    n = s.n
+    rF = (1e-3 * rng.normal(size=(n, 3, 3))).astype(np.float32)
+    rx = (1e-3 * rng.normal(size=(n, 3))).astype(np.float32)
+    return w, s, g, tgt, prm, rF, rx
+
+
+def make_single():
+    """OptimizeSingleTimestep (CompGraph.cpp:369-465) as run.py's E2E path
+    calls it, both builds, each in a fresh process: the reference's Adam step
+    counter is a function-local static that starts at 0 and carries over
+    between calls (CompGraph.cpp:396)."""
+    import subprocess
+    for bits in (64, 32):
+        subprocess.check_call([sys.executable, __file__, "--single-bits", str(bits)])
+    rec = dict(np.load(OUT / "reference_single_64.npz"))
+    rec.update(np.load(OUT / "reference_single_32.npz"))
+    (OUT / "reference_single_64.npz").unlink()
+    (OUT / "reference_single_32.npz").unlink()
+    np.savez_compressed(OUT / "reference_single.npz", **rec)
+    print("wrote", OUT / "reference_single.npz")
+
+
+def _make_single_bits(bits):
+    ref = O.Reference(bits)
+    w, s, g, tgt, prm, rF, rx = single_case()
+    dfc, xT, loss, log = ref.optimize_single(g, prm, s, tgt, SINGLE_LAYERS, SINGLE_CALLS, rF, rx)
+    accepted = [int(line.split("ls_iter=")[1].split(",")[0]) if "accepted" in line else -1
+                for line in log.splitlines() if "Step accepted" in line or "Line search failed" in line]
+    rec = {f"single{bits}_dFc": dfc, f"single{bits}_xT": xT, f"single{bits}_loss": loss,
+           f"single{bits}_ls": np.asarray(accepted)}
+    if bits == 64:
+        rec.update(dims=np.asarray(w.dims), dx=w.dx, dt=prm.dt, drag=prm.drag, smoothing=prm.smoothing, target=tgt,
+                   x=s.x, v=s.v, m=s.m, vol=s.vol, lam=s.lam, mu=s.mu, render_dLdF=rF, render_dLdx=rx,
+                   calls=np.asarray(SINGLE_CALLS, np.float64), layers=SINGLE_LAYERS)
+    np.savez(OUT / f"reference_single_{bits}.npz", **rec)
+    print(bits, "losses", loss, "line-search outcomes", accepted)
+
+
+def main(which=("small", "optimize", "mesh", "single")):
     build_oracle.build_oracle()
     outs = build_oracle.build_ref()
     if not outs:
@@ -138,6 +191,8 @@ def main(which=("small", "optimize", "mesh")):
         make_optimize()
     if "mesh" in which:
         make_mesh_sampling()
+    if "single" in which:
+        make_single()
     if "small" not in which:
         return
     r64, r32 = O.Reference(64), O.Reference(32)
@@ -215,6 +270,10 @@ def main(which=("small", "optimize", "mesh")):
 if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["small", "optimize", "mesh"])
+    ap.add_argument("--only", choices=["small", "optimize", "mesh", "single"])
+    ap.add_argument("--single-bits", type=int, choices=[32, 64], help=argparse.SUPPRESS)
     a = ap.parse_args()
-    main((a.only,) if a.only else ("small", "optimize", "mesh"))
+    if a.single_bits:
+        _make_single_bits(a.single_bits)
+    else:
+        main((a.only,) if a.only else ("small", "optimize", "mesh", "single"))

@@ -8,9 +8,12 @@ control dFc and the final positions.
 FP64 engine: to 1e-9.  FP32 engine (default and deterministic scatters):
 the same curve, same accept/reject decisions, within 1e-4 relative -- the
 reference's own float build lands 3e-5 from its double build here."""
+from pathlib import Path
+
 import numpy as np
 import pytest
 
+import oracle as O
 from helpers import golden_opt_case, make_graph, rel_err
 
 pytestmark = pytest.mark.gpu
@@ -104,3 +107,68 @@ def test_control_episode_twin_loss_curve(dm, orc):
     assert len(got) == len(want)
     assert np.abs(got - want).max() <= 1e-4 * want.max()
     assert got[-1] < got[0]
+
+
+def _single(dm, precision):
+    """run.py's E2E physics path on the GPU with the fixture's inputs: layers,
+    a forward pass, stored render gradients, then the fixture's calls of
+    optimize_single_timestep.  Per call: every layer's dFc, the last
+    positions, the end-layer loss and the losses the call evaluated."""
+    gs = dict(np.load(Path(__file__).resolve().parent / "golden" / "reference_single.npz"))
+    n = len(gs["m"])
+    s = O.State(gs["x"], gs["v"], np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), gs["m"], gs["vol"],
+                gs["lam"], gs["mu"])
+    g = O.Grid(tuple(int(d) for d in gs["dims"]), float(gs["dx"]))
+    prm = O.Params(dt=float(gs["dt"]), drag=float(gs["drag"]), smoothing=float(gs["smoothing"]))
+    L = int(gs["layers"])
+    cg, keep = make_graph(dm, s, g, prm, precision=precision, layers=1, target_mass=gs["target"])
+    cg.set_up_comp_graph(L)
+    cg.compute_forward_pass(0, 0)
+    cg.set_render_gradients(gs["render_dLdF"], gs["render_dLdx"])
+    dm.single_timestep_adam_step(set_to=0)  # as in a fresh reference process
+    out = []
+    for t, gd, alpha, ls in gs["calls"]:
+        # the reference's double build takes alpha as a double: bypass the
+        # binding's float32 rounding of initial_alpha for the FP64 engine
+        a = float(alpha) if precision == "fp64" else float(np.float32(alpha))
+        dm._lib.check(dm._lib.lib.mpm_compgraph_optimize_single_timestep(cg._h, int(t), int(gd), 0, a, int(ls)))
+        hist = cg.loss_history()
+        dfc = np.stack([cg.get_point_cloud(i).get("dFc", np.float64) for i in range(L)])
+        xT = cg.get_point_cloud(L - 1).get("x", np.float64)
+        out.append((dfc, xT, cg.end_layer_mass_loss(), hist))
+    return gs, out, dm.single_timestep_adam_step()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_single_timestep_optimizer_matches_reference(dm, orc, precision):
+    """optimize_single_timestep (OptimizeSingleTimestep, CompGraph.cpp:369-465;
+    bind.cpp:294-317), the call run.py's E2E mode makes (run.py:686), with
+    render gradients injected at every backward (CompGraph.cpp:148-197),
+    against the reference's recorded calls and the oracle's restatement of
+    them, loss by loss.  FP64 engine to 1e-9; FP32 engine within 1e-4 with
+    the same accept/reject decisions (the reference's float build is ~1e-6
+    from its double build on these losses)."""
+    gs, out, adam_steps = _single(dm, precision)
+    n = len(gs["m"])
+    s = O.State(gs["x"], gs["v"], np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), gs["m"], gs["vol"],
+                gs["lam"], gs["mu"])
+    og = O.OracleGraph(orc, O.Grid(tuple(int(d) for d in gs["dims"]), float(gs["dx"])),
+                       O.Params(dt=float(gs["dt"]), drag=float(gs["drag"]), smoothing=float(gs["smoothing"])),
+                       s, gs["target"])
+    O.OracleGraph.adam_step = 0
+    og.set_up(int(gs["layers"]))
+    og.forward(0)
+    og.set_render_gradients(gs["render_dLdF"].astype(np.float64), gs["render_dLdx"].astype(np.float64))
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    for c, ((dfc, xT, loss, hist), (t, gd, alpha, ls)) in enumerate(zip(out, gs["calls"])):
+        og.history = []
+        og.optimize_single_timestep(int(t), int(gd), 0, float(alpha), int(ls))
+        want_hist = np.asarray(og.history)
+        assert len(hist) == len(want_hist), (c, hist, want_hist)
+        e_hist = float(np.abs(hist - want_hist).max() / np.abs(want_hist).max())
+        e_dfc = rel_err(dfc, gs["single64_dFc"][c])
+        e_loss = abs(loss - gs["single64_loss"][c]) / abs(gs["single64_loss"][c])
+        print(f"{precision} call {c}: losses {e_hist:.2e}, dFc {e_dfc:.2e}, end loss {e_loss:.2e}")
+        assert e_hist < tol and e_dfc < tol and e_loss < tol, (c, e_hist, e_dfc, e_loss)
+        assert rel_err(xT, gs["single64_xT"][c]) < (1e-11 if precision == "fp64" else 1e-6)
+    assert adam_steps == O.OracleGraph.adam_step == int((gs["single64_ls"] >= 0).sum())

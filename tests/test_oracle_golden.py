@@ -1,6 +1,8 @@
 """The FP64 oracle against golden vectors recorded from the reference's own
 sources (tests/golden/reference_small.npz, made by tests/golden/make_golden.py
 from DiffMPMLib3D compiled with float widened to double)."""
+from pathlib import Path
+
 import numpy as np
 
 import oracle as O
@@ -116,3 +118,28 @@ def test_mesh_sampling_oracle_matches_reference():
         ref_set = {tuple(p) for p in ref.astype(np.float32).tolist()}
         want = np.array([tuple(p) in ref_set for p in sub.tolist()])
         assert (keep == want).all(), name
+
+
+def test_single_timestep_optimiser_matches_reference(orc):
+    """OptimizeSingleTimestep as run.py's E2E path calls it (layers, a forward
+    pass, stored render gradients, then four calls at layers 2, 0, 2, 4):
+    the oracle's restatement against the reference's double build, call by
+    call -- every layer's dFc, the last positions and the end-layer loss."""
+    gs = dict(np.load(Path(__file__).resolve().parent / "golden" / "reference_single.npz"))
+    n = len(gs["m"])
+    s = O.State(gs["x"], gs["v"], np.zeros((n, 3, 3)), np.tile(np.eye(3), (n, 1, 1)), gs["m"], gs["vol"],
+                gs["lam"], gs["mu"])
+    g = O.Grid(tuple(int(d) for d in gs["dims"]), float(gs["dx"]))
+    prm = O.Params(dt=float(gs["dt"]), drag=float(gs["drag"]), smoothing=float(gs["smoothing"]))
+    og = O.OracleGraph(orc, g, prm, s, gs["target"])
+    O.OracleGraph.adam_step = 0  # the reference's counter in a fresh process
+    og.set_up(int(gs["layers"]))
+    og.forward(0)
+    og.set_render_gradients(gs["render_dLdF"].astype(np.float64), gs["render_dLdx"].astype(np.float64))
+    for c, (t, gd, alpha, ls) in enumerate(gs["calls"]):
+        og.optimize_single_timestep(int(t), int(gd), 0, float(alpha), int(ls))
+        dfc = np.stack([lay.dFc for lay in og.layers])
+        assert rel_err(dfc, gs["single64_dFc"][c]) < 1e-11, c
+        assert rel_err(og.layers[-1].x, gs["single64_xT"][c]) < 1e-13, c
+        assert abs(og.loss() - gs["single64_loss"][c]) < 1e-12 * abs(gs["single64_loss"][c]), c
+    assert O.OracleGraph.adam_step == int((gs["single64_ls"] >= 0).sum())
