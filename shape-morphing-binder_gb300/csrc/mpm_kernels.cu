@@ -1206,6 +1206,112 @@ __global__ void k_grid_adj(KP<R> kp, long long nn, const R* __restrict__ grid, R
     }
 }
 
+// The P2G-transpose gather (FP32 tile or global reads).  TILE: every node
+// of the block's stencils is in the staged tile, which holds zeros outside
+// the grid, so the per-node grid bounds checks are not needed.
+template <typename R, int K, bool TILE>
+MPM_D void p2g_adj_gather(const KP<R>& kp, const Stencil<R, K>& sn, const GTile& tl, const float4* ta, const float4* tg,
+                          const R* __restrict__ adj, const R* __restrict__ grid, R mass, const R* mvv, const R* A,
+                          const R* vbar, const R* CC, R* M1, R* ax, R* bp, R* bv)
+{
+    // Separable accumulation over the K^3 stencil.  Per node n = (a,b,c) with
+    // d = (dL/dp, dL/dm) and v_i the node velocity:
+    //   sig_n = m dL/dm + (m v' + A dg).dL/dp + v_i.(vbar + C0 Cbar dg)
+    //   ax += sig_n grad w_n,  bp += w_n dL/dp,  bv += w_n v_i,
+    //   M1 += w_n dL/dp dg^T
+    // with w_n = wx_a wy_b wz_c and grad w_n = -(1/dx)(sx wy wz, wx sy wz,
+    // wx wy sz); the sums over c, then b, are folded into per-(a,b) and
+    // per-a partials so each node costs ~24 FMAs.
+#pragma unroll
+    for (int a = 0; a < K; ++a) {
+        const int i = sn.base[0] + a;
+        if (!TILE && (unsigned)i >= (unsigned)kp.dims[0]) continue;
+        const R gxa = sn.g[0][a];
+        R Pa[3], Qa[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            Pa[r] = mvv[r] + A[r * 3] * gxa;
+            Qa[r] = vbar[r] + CC[r * 3] * gxa;
+        }
+        R Tw[3] = {0, 0, 0}, Tv[3] = {0, 0, 0}, Tgy[3] = {0, 0, 0}, Tgz[3] = {0, 0, 0};
+        R Sww = 0, Ssw = 0, Sws = 0;
+#pragma unroll
+        for (int b = 0; b < K; ++b) {
+            const int j = sn.base[1] + b;
+            if (!TILE && (unsigned)j >= (unsigned)kp.dims[1]) continue;
+            const R gyb = sn.g[1][b];
+            R Pab[3], Qab[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                Pab[r] = Pa[r] + A[r * 3 + 1] * gyb;
+                Qab[r] = Qa[r] + CC[r * 3 + 1] * gyb;
+            }
+            R U[3] = {0, 0, 0}, UV[3] = {0, 0, 0}, Ug[3] = {0, 0, 0};
+            R Vw = 0, Vs = 0;
+            const long long row = TILE ? 0 : ((long long)i * kp.dims[1] + j) * kp.dims[2];
+            const int trow = TILE ? tl.index(i, j, 0) : 0;  // + k gives index(i, j, k)
+#pragma unroll
+            for (int c = 0; c < K; ++c) {
+                const int k = sn.base[2] + c;
+                if (!TILE && (unsigned)k >= (unsigned)kp.dims[2]) continue;
+                R d[4], vi[3];
+                if constexpr (TILE) {
+                    const float4 qa = ta[trow + k], qg = tg[trow + k];
+                    d[0] = (R)qa.x;
+                    d[1] = (R)qa.y;
+                    d[2] = (R)qa.z;
+                    d[3] = (R)qa.w;
+                    vi[0] = (R)qg.x;
+                    vi[1] = (R)qg.y;
+                    vi[2] = (R)qg.z;
+                } else {
+                    load_node4(adj, row + k, d);
+                    load_node3(grid, row + k, vi);
+                }
+                const R gzc = sn.g[2][c], wc = sn.w[2][c];
+                R sig = mass * d[3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    sig += (Pab[r] + A[r * 3 + 2] * gzc) * d[r];
+                    sig += vi[r] * (Qab[r] + CC[r * 3 + 2] * gzc);
+                }
+                const R wcg = wc * gzc;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    U[r] += wc * d[r];
+                    UV[r] += wc * vi[r];
+                    Ug[r] += wcg * d[r];
+                }
+                Vw += wc * sig;
+                Vs += sn.s[2][c] * sig;
+            }
+            const R wb = sn.w[1][b], wbg = wb * gyb;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                Tw[r] += wb * U[r];
+                Tv[r] += wb * UV[r];
+                Tgy[r] += wbg * U[r];
+                Tgz[r] += wb * Ug[r];
+            }
+            Sww += wb * Vw;
+            Ssw += sn.s[1][b] * Vw;
+            Sws += wb * Vs;
+        }
+        const R wa = sn.w[0][a], wag = wa * gxa;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            bp[r] += wa * Tw[r];
+            bv[r] += wa * Tv[r];
+            M1[r * 3 + 0] += wag * Tw[r];
+            M1[r * 3 + 1] += wa * Tgy[r];
+            M1[r * 3 + 2] += wa * Tgz[r];
+        }
+        ax[0] += sn.s[0][a] * Sww;
+        ax[1] += wa * Ssw;
+        ax[2] += wa * Sws;
+    }
+}
+
 // P2G^T + P_op_1^T (BackPropagation.cpp:76-143)
 template <typename R, int K>
 __global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP<R> kp, int n, long long ld, const R* __restrict__ st,
@@ -1265,102 +1371,14 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_ADJ_MIN_BLOCKS) k_p2g_adj(KP
         tl = stage_gather_tile<K, 2>(kp, true, sn.base, reinterpret_cast<const float4*>(adj),
                                      reinterpret_cast<const float4*>(grid), ta, tg, cap);
     }
-    // Separable accumulation over the K^3 stencil.  Per node n = (a,b,c) with
-    // d = (dL/dp, dL/dm) and v_i the node velocity:
-    //   sig_n = m dL/dm + (m v' + A dg).dL/dp + v_i.(vbar + C0 Cbar dg)
-    //   ax += sig_n grad w_n,  bp += w_n dL/dp,  bv += w_n v_i,
-    //   M1 += w_n dL/dp dg^T
-    // with w_n = wx_a wy_b wz_c and grad w_n = -(1/dx)(sx wy wz, wx sy wz,
-    // wx wy sz); the sums over c, then b, are folded into per-(a,b) and
-    // per-a partials so each node costs ~24 FMAs.
     R M1[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ax[3] = {0, 0, 0}, bp[3] = {0, 0, 0}, bv[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < K; ++a) {
-        const int i = sn.base[0] + a;
-        if ((unsigned)i >= (unsigned)kp.dims[0]) continue;
-        const R gxa = sn.g[0][a];
-        R Pa[3], Qa[3];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            Pa[r] = mvv[r] + A[r * 3] * gxa;
-            Qa[r] = o.vbar[r] + CC[r * 3] * gxa;
-        }
-        R Tw[3] = {0, 0, 0}, Tv[3] = {0, 0, 0}, Tgy[3] = {0, 0, 0}, Tgz[3] = {0, 0, 0};
-        R Sww = 0, Ssw = 0, Sws = 0;
-#pragma unroll
-        for (int b = 0; b < K; ++b) {
-            const int j = sn.base[1] + b;
-            if ((unsigned)j >= (unsigned)kp.dims[1]) continue;
-            const R gyb = sn.g[1][b];
-            R Pab[3], Qab[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                Pab[r] = Pa[r] + A[r * 3 + 1] * gyb;
-                Qab[r] = Qa[r] + CC[r * 3 + 1] * gyb;
-            }
-            R U[3] = {0, 0, 0}, UV[3] = {0, 0, 0}, Ug[3] = {0, 0, 0};
-            R Vw = 0, Vs = 0;
-            const long long row = ((long long)i * kp.dims[1] + j) * kp.dims[2];
-            const int trow = tl.on ? tl.index(i, j, 0) : 0;  // + k gives index(i, j, k)
-#pragma unroll
-            for (int c = 0; c < K; ++c) {
-                const int k = sn.base[2] + c;
-                if ((unsigned)k >= (unsigned)kp.dims[2]) continue;
-                R d[4], vi[3];
-                if (tl.on) {
-                    const float4 qa = ta[trow + k], qg = tg[trow + k];
-                    d[0] = (R)qa.x;
-                    d[1] = (R)qa.y;
-                    d[2] = (R)qa.z;
-                    d[3] = (R)qa.w;
-                    vi[0] = (R)qg.x;
-                    vi[1] = (R)qg.y;
-                    vi[2] = (R)qg.z;
-                } else {
-                    load_node4(adj, row + k, d);
-                    load_node3(grid, row + k, vi);
-                }
-                const R gzc = sn.g[2][c], wc = sn.w[2][c];
-                R sig = mass * d[3];
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    sig += (Pab[r] + A[r * 3 + 2] * gzc) * d[r];
-                    sig += vi[r] * (Qab[r] + CC[r * 3 + 2] * gzc);
-                }
-                const R wcg = wc * gzc;
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    U[r] += wc * d[r];
-                    UV[r] += wc * vi[r];
-                    Ug[r] += wcg * d[r];
-                }
-                Vw += wc * sig;
-                Vs += sn.s[2][c] * sig;
-            }
-            const R wb = sn.w[1][b], wbg = wb * gyb;
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                Tw[r] += wb * U[r];
-                Tv[r] += wb * UV[r];
-                Tgy[r] += wbg * U[r];
-                Tgz[r] += wb * Ug[r];
-            }
-            Sww += wb * Vw;
-            Ssw += sn.s[1][b] * Vw;
-            Sws += wb * Vs;
-        }
-        const R wa = sn.w[0][a], wag = wa * gxa;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            bp[r] += wa * Tw[r];
-            bv[r] += wa * Tv[r];
-            M1[r * 3 + 0] += wag * Tw[r];
-            M1[r * 3 + 1] += wa * Tgy[r];
-            M1[r * 3 + 2] += wa * Tgz[r];
-        }
-        ax[0] += sn.s[0][a] * Sww;
-        ax[1] += wa * Ssw;
-        ax[2] += wa * Sws;
+    if constexpr (sizeof(R) == 4) {
+        if (tl.on)
+            p2g_adj_gather<R, K, true>(kp, sn, tl, ta, tg, adj, grid, mass, mvv, A, o.vbar, CC, M1, ax, bp, bv);
+        else
+            p2g_adj_gather<R, K, false>(kp, sn, tl, ta, tg, adj, grid, mass, mvv, A, o.vbar, CC, M1, ax, bp, bv);
+    } else {
+        p2g_adj_gather<R, K, false>(kp, sn, tl, ta, tg, adj, grid, mass, mvv, A, o.vbar, CC, M1, ax, bp, bv);
     }
     {
         const R nidx = -kp.inv_dx;
