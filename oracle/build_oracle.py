@@ -133,6 +133,48 @@ def build_ref(force: bool = False) -> list[Path]:
     return outs
 
 
+def build_ref_module(widen: bool = False, force: bool = False) -> Path | None:
+    """The reference's own Python module, ``diffmpm_bindings`` (bind/bind.cpp
+    and the DiffMPMLib3D sources, without its optional torch support),
+    compiled with g++ and pybind11: float as shipped into
+    ``oracle/_ref/pymod32/``, or with float widened to double (bind.cpp
+    included, on temporary copies) into ``oracle/_ref/pymod64/``.  Only
+    tests/golden/run_py_sequence.py imports it, to record what the reference
+    returns for run.py's call sequence."""
+    ref = ref_dir()
+    if ref is None or not (ref / "bind" / "bind.cpp").exists():
+        return None
+    try:
+        import pybind11
+    except ImportError:
+        return None
+    import sysconfig
+    out_dir = OUT_REF / ("pymod64" if widen else "pymod32")
+    out = out_dir / ("diffmpm_bindings" + sysconfig.get_config_var("EXT_SUFFIX"))
+    inputs = [ref / "DiffMPMLib3D" / s for s in REF_SOURCES] + [ref / "bind" / "bind.cpp", Path(__file__)]
+    if not force and _newer(out, inputs):
+        return out
+    out_dir.mkdir(parents=True, exist_ok=True)
+    tmp = Path(tempfile.mkdtemp(prefix="mpm_refmod_"))
+    try:
+        src = _stage(tmp, widen, ref)
+        bind = (ref / "bind" / "bind.cpp").read_text(encoding="utf-8", errors="replace")
+        (src / "bind.cpp").write_text(_widen(bind) if widen else bind, encoding="utf-8")
+        inc = ["-I", str(src), "-I", str(ref / "include"), "-I", str(ref / "include" / "qrsvd"),
+               "-I", pybind11.get_include(), "-I", sysconfig.get_paths()["include"]]
+        objs, jobs = [], []
+        for name in REF_SOURCES + ["bind.cpp"]:
+            obj = tmp / (name + ".o")
+            objs.append(obj)
+            jobs.append((["g++", *CXXFLAGS, "-fvisibility=hidden", *inc, "-c", str(src / name), "-o", str(obj)],))
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+            list(ex.map(_compile, jobs))
+        subprocess.check_call(["g++", "-shared", "-fopenmp", *map(str, objs), "-o", str(out)])
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--no-ref", action="store_true")
