@@ -747,7 +747,8 @@ __device__ GTile stage_gather_tile(const KP<float>& kp, bool valid, const int* b
 // J trust region, F update with smoothing, advection, stores of layer n+1.
 template <typename R>
 MPM_D void g2p_finish(const KP<R>& kp, long long ld, int p, const R* x, const R* F, const R* Ft, const R* vs,
-                      const R* Cx, const R* Cy, const R* Cz, R* __restrict__ st1, R* __restrict__ trust)
+                      const R* Cx, const R* Cy, const R* Cz, R* __restrict__ st1, R* __restrict__ trust,
+                      R* x_out = nullptr, R* C_out = nullptr, R* F_out = nullptr)
 {
     R Cn[9];
 #pragma unroll
@@ -786,42 +787,45 @@ MPM_D void g2p_finish(const KP<R>& kp, long long ld, int p, const R* x, const R*
     store_planes(st1 + ST_C * ld, ld, p, 9, Cn);
     store_planes(st1 + ST_F * ld, ld, p, 9, Fn);
     if (trust) trust[p] = s_tr;
+    // the new state, for a caller that goes on with it (the fused G2P->P2G)
+    if (x_out)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) x_out[a] = x1[a];
+    if (C_out)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) C_out[i] = Cn[i];
+    if (F_out)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) F_out[i] = Fn[i];
 }
 
-template <typename R, int K>
-__global__ void __launch_bounds__(kThreads, MPM_G2P_MIN_BLOCKS) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
-                                                   const R* __restrict__ dfc, const R* __restrict__ grid,
-                                                   R* __restrict__ st1, R* __restrict__ trust)
+// G2P gather: v = sum w v_i, Cacc[:,a] = sum w v_i dg_a, separable.
+// CHECK = false for a particle whose whole stencil lies inside the grid (the
+// common case): no per-node bounds checks, so every node load can issue
+// without waiting on a predicate.
+template <typename R, int K, bool CHECK>
+MPM_D void g2p_gather(const KP<R>& kp, const Stencil<R, K>& sn, const R* __restrict__ grid, R* vs, R* Cx, R* Cy,
+                      R* Cz)
 {
-    long long goff;
-    bind_instance(kp, n, goff);
-    grid += goff * 4;
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    R x[3], F[9], Ft[9];
-    load_planes(st + ST_X * ld, ld, p, 3, x);
-    load_Ft(st, dfc, ld, p, F, Ft);
-    Stencil<R, K> sn;
-    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
-    // separable accumulation: v = sum w v_i, Cacc[:,a] = sum w v_i dg_a
-    R vs[3] = {0, 0, 0}, Cx[3] = {0, 0, 0}, Cy[3] = {0, 0, 0}, Cz[3] = {0, 0, 0};
+    const long long sy = kp.dims[2], sx = (long long)kp.dims[1] * kp.dims[2];
+    const long long base = ((long long)sn.base[0] * kp.dims[1] + sn.base[1]) * kp.dims[2] + sn.base[2];
 #pragma unroll
     for (int a = 0; a < K; ++a) {
         const int i = sn.base[0] + a;
-        if ((unsigned)i >= (unsigned)kp.dims[0]) continue;
+        if (CHECK && (unsigned)i >= (unsigned)kp.dims[0]) continue;
         R t0[3] = {0, 0, 0}, t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
 #pragma unroll
         for (int b = 0; b < K; ++b) {
             const int j = sn.base[1] + b;
-            if ((unsigned)j >= (unsigned)kp.dims[1]) continue;
+            if (CHECK && (unsigned)j >= (unsigned)kp.dims[1]) continue;
             R s0[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
-            const long long row = ((long long)i * kp.dims[1] + j) * kp.dims[2];
+            const long long row = base + a * sx + b * sy;
 #pragma unroll
             for (int c = 0; c < K; ++c) {
                 const int k = sn.base[2] + c;
-                if ((unsigned)k >= (unsigned)kp.dims[2]) continue;
+                if (CHECK && (unsigned)k >= (unsigned)kp.dims[2]) continue;
                 R vi[3];
-                load_node3(grid, row + k, vi);
+                load_node3(grid, row + c, vi);
                 const R wz = sn.w[2][c], wzg = wz * sn.g[2][c];
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
@@ -846,6 +850,36 @@ __global__ void __launch_bounds__(kThreads, MPM_G2P_MIN_BLOCKS) k_g2p(KP<R> kp, 
             Cz[r] += wx * t2[r];
         }
     }
+}
+
+template <typename R, int K>
+MPM_D bool stencil_inside(const KP<R>& kp, const Stencil<R, K>& sn)
+{
+    bool in = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) in &= sn.base[a] >= 0 && sn.base[a] + K <= kp.dims[a];
+    return in;
+}
+
+template <typename R, int K>
+__global__ void __launch_bounds__(kThreads, MPM_G2P_MIN_BLOCKS) k_g2p(KP<R> kp, int n, long long ld, const R* __restrict__ st,
+                                                   const R* __restrict__ dfc, const R* __restrict__ grid,
+                                                   R* __restrict__ st1, R* __restrict__ trust)
+{
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    R x[3], F[9], Ft[9];
+    load_planes(st + ST_X * ld, ld, p, 3, x);
+    load_Ft(st, dfc, ld, p, F, Ft);
+    Stencil<R, K> sn;
+    make_stencil<R, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+    R vs[3] = {0, 0, 0}, Cx[3] = {0, 0, 0}, Cy[3] = {0, 0, 0}, Cz[3] = {0, 0, 0};
+    // (the plain FP64 form keeps one checked path)
+    if (sizeof(R) == 4 && stencil_inside(kp, sn)) g2p_gather<R, K, false>(kp, sn, grid, vs, Cx, Cy, Cz);
+    else g2p_gather<R, K, true>(kp, sn, grid, vs, Cx, Cy, Cz);
     g2p_finish(kp, ld, p, x, F, Ft, vs, Cx, Cy, Cz, st1, trust);
 }
 
