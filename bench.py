@@ -135,6 +135,9 @@ class Clocks:
 # storage)
 KERNEL_BYTES = {
     "p2g": (112, 16),
+    # G2P of a step fused with the next step's P2G: G2P's bytes plus the
+    # particle constants; the state it writes is not read back
+    "g2p2g": (164, 32),
     "g2p": (148, 16),
     "g2p_adj": (184, 16),
     "p2g_adj": (380, 32),
@@ -267,7 +270,7 @@ def run_ours(args, rank, world, device):
     lib.mpm_profile_enable(0)
     kern = {}
     import ctypes as C
-    for k in range(10):
+    for k in range(11):
         cnt, ms = C.c_longlong(), C.c_double()
         lib.mpm_profile_query(k, C.byref(cnt), C.byref(ms))
         if cnt.value:

@@ -125,6 +125,13 @@ int mpm_set_tile_nodes(int nodes);
  * warp per run of particles sharing a cell, one lane per stencil node; the
  * default), 0 = one thread per particle */
 int mpm_set_scatter_mode(int mode);
+/* No counterpart in the reference (whose ForwardTimeStep runs P2G, the grid
+ * update and G2P one after another, ForwardSimulation.cpp:159-185): forward
+ * passes in FP32 with float scatters run each step's G2P fused with the next
+ * step's P2G, which then takes the new particle state from registers instead
+ * of reading it back (1, the default); 0 runs the steps one by one.  The
+ * computation is the same either way. */
+int mpm_set_fused_steps(int on);
 /* CalculateLameParameters (Elasticity.cpp:149-153; bind.cpp:540-544) */
 int mpm_lame(double young, double poisson, double* lam, double* mu);
 
@@ -272,7 +279,9 @@ int mpm_constitutive(int n, int precision, int material, int adjoint, const doub
 /* ---------------------------------------------------------- measurement */
 /* kernel ids for the profiler */
 enum { MPM_K_P2G = 0, MPM_K_GRID_UPDATE = 1, MPM_K_G2P = 2, MPM_K_G2P_ADJ = 3, MPM_K_GRID_ADJ = 4,
-       MPM_K_P2G_ADJ = 5, MPM_K_LOSS = 6, MPM_K_ADAM = 7, MPM_K_NORM = 8, MPM_K_COUNT = 10 };
+       MPM_K_P2G_ADJ = 5, MPM_K_LOSS = 6, MPM_K_ADAM = 7, MPM_K_NORM = 8,
+       MPM_K_G2P2G = 10, /* G2P of a step fused with the next step's P2G */
+       MPM_K_COUNT = 11 };
 /* record CUDA events around every kernel launch on its stream (1 = on) */
 int mpm_profile_enable(int on);
 int mpm_profile_reset(void);

@@ -85,10 +85,11 @@ void say(const char* fmt, ...)
 // Optional CUDA-event timing of every kernel the engine launches, recorded on
 // the stream the kernel runs on, plus a running launch counter.
 enum {
-    K_P2G = 0, K_GRID_UPDATE, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_LOSS, K_ADAM, K_NORM, K_AUX, K_COUNT
+    K_P2G = 0, K_GRID_UPDATE, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_LOSS, K_ADAM, K_NORM, K_AUX, K_G2P2G,
+    K_COUNT
 };
 const char* k_names[K_COUNT] = {"p2g", "grid_update", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "mass_loss",
-                                "adam", "grad_norm", "aux"};
+                                "adam", "grad_norm", "aux", "g2p2g"};
 
 struct Prof {
     bool on = false;
@@ -529,7 +530,7 @@ struct Graph {
     cudaStream_t own = nullptr, stream = nullptr;
     // scratch
     Buf adj, lgm, ldm, acc;
-    Buf fgrid, ftrust;                              // checkpointed forward
+    Buf fgrid, fgrid2, ftrust;                      // checkpointed forward (two grids: fused steps)
     std::shared_ptr<PCData> ping, pong;             // non-stored forward states
     std::vector<std::shared_ptr<PCData>> seg;       // recomputed segment states
     std::vector<Buf> sgrid, strust;                 // recomputed segment grids
@@ -605,6 +606,7 @@ struct Graph {
         c.exact = opt.adjoint == MPM_ADJ_EXACT;
         c.tile_nodes = tile_nodes;
         c.scatter_mode = scatter_mode;
+        c.fuse = g_fuse_steps;
         c.adj_tile_nodes = adj_tile_nodes;
         c.gather_tile_nodes = gather_tile_nodes;
         double max_dx = geom.dx;
@@ -810,6 +812,73 @@ void step_forward(const StepCfg& c, PCData& a, PCData& b, Buf& grid, Buf& trust,
     b.have_state = true;
 }
 
+// A run of consecutive forward steps: step k advances a[k] -> b[k] with its
+// own grid and trust buffers, and b[k] is a[k+1].  Where the configuration
+// allows (FP32, float atomics, segmented scatter) the G2P of step k and the
+// P2G of step k+1 run as one fused kernel, so the state written for layer
+// k+1 is not read back; the grids of consecutive steps must then be distinct
+// buffers (the caller's plan guarantees it).  The computation is the same as
+// step_forward run step by step.
+struct StepBufs {
+    PCData* a;
+    PCData* b;
+    Buf* grid;
+    Buf* trust;
+};
+
+template <typename R>
+void run_forward_steps(const StepCfg& c, const std::vector<StepBufs>& plan, cudaStream_t s)
+{
+    const int m = (int)plan.size();
+    if (m == 0) return;
+    if (m == 1 || !g2p2g_applies(c, (int)sizeof(R))) {
+        for (const auto& st : plan) step_forward<R>(c, *st.a, *st.b, *st.grid, *st.trust, s);
+        return;
+    }
+    const long long nn = c.nodes();
+    auto prep_grid = [&](Buf& g) {
+        ensure(g, sizeof(R) * 4 * nn, s, false);
+        ck(cudaMemsetAsync(g->p, 0, sizeof(R) * 4 * nn, s), "grid reset");
+    };
+    // the first step's P2G on its own
+    {
+        PCData& a = *plan[0].a;
+        prep_grid(*plan[0].grid);
+        const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
+        KTimer kt(K_P2G, s);
+        launch_p2g<R>(c, a.n, a.ld, a.st->as<R>(), dfc, a.co->as<R>(), (*plan[0].grid)->as<R>(), s);
+    }
+    check_launch("p2g");
+    for (int k = 0; k < m; ++k) {
+        ++g_fwd_steps;
+        const StepBufs& st = plan[k];
+        PCData& a = *st.a;
+        PCData& b = *st.b;
+        {
+            KTimer kt(K_GRID_UPDATE, s);
+            launch_grid_update<R>(c, (*st.grid)->as<R>(), s);
+        }
+        check_launch("grid_update");
+        const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
+        R* tr = nullptr;
+        if (c.exact) tr = ensure(*st.trust, sizeof(R) * a.ld, s, false)->as<R>();
+        if (!b.st) b.st = make_buf(a.planes_bytes(ST_N), s, false);
+        if (k + 1 < m) {
+            prep_grid(*plan[k + 1].grid);
+            KTimer kt(K_G2P2G, s);
+            if constexpr (sizeof(R) == 4)
+                launch_g2p2g(c, a.n, a.ld, a.st->as<float>(), dfc, a.co->as<float>(), (*st.grid)->as<float>(),
+                             b.st->as<float>(), tr, (*plan[k + 1].grid)->as<float>(), s);
+        } else {
+            KTimer kt(K_G2P, s);
+            launch_g2p<R>(c, a.n, a.ld, a.st->as<R>(), dfc, (*st.grid)->as<R>(), b.st->as<R>(), tr, s);
+        }
+        check_launch(k + 1 < m ? "g2p2g" : "g2p");
+        b.dfc_zero = true;
+        b.have_state = true;
+    }
+}
+
 // One adjoint step: grads of layer i+1 -> grads of layer i (BackPropagation.cpp:9-144)
 template <typename R>
 void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& grid, const Buf& trust,
@@ -1001,6 +1070,7 @@ void graph_forward(Graph& G, int start)
     sig.add_pc(G.ping.get());
     sig.add_pc(G.pong.get());
     sig.add(G.fgrid);
+    sig.add(G.fgrid2);
     sig.add(G.ftrust);
     // checkpointed: the last segment's states, grids and trust scales go to
     // the segment scratch, where the backward pass will look for them
@@ -1022,6 +1092,7 @@ void graph_forward(Graph& G, int start)
     run_captured(G, "fwd" + std::to_string(start), sig, [&]() {
         PCData* cur = G.layers[start].pc.get();
         begin_fix_pass(G, c, *cur, s);
+        std::vector<StepBufs> plan;
         for (int i = start; i < L - 1; ++i) {
             PCData* nxt;
             const bool in_tail = keep_tail && i >= tail_lo;
@@ -1038,11 +1109,12 @@ void graph_forward(Graph& G, int start)
                 if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
                 nxt = tmp.get();
             }
-            if (full) step_forward<R>(c, *cur, *nxt, G.layers[i].grid, G.layers[i].trust, s);
-            else if (in_tail) step_forward<R>(c, *cur, *nxt, G.sgrid[i - tail_lo], G.strust[i - tail_lo], s);
-            else step_forward<R>(c, *cur, *nxt, G.fgrid, G.ftrust, s);
+            if (full) plan.push_back({cur, nxt, &G.layers[i].grid, &G.layers[i].trust});
+            else if (in_tail) plan.push_back({cur, nxt, &G.sgrid[i - tail_lo], &G.strust[i - tail_lo]});
+            else plan.push_back({cur, nxt, ((i - start) & 1) ? &G.fgrid2 : &G.fgrid, &G.ftrust});
             cur = nxt;
         }
+        run_forward_steps<R>(c, plan, s);
     });
     // layer flags set by the steps (replays do not run the host code)
     for (int i = start + 1; i < L; ++i)
@@ -1170,10 +1242,14 @@ void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cu
         if (!G.ping || G.ping->n != S[0]->n) G.ping = shell_like(*S[0], s, true);
         // the last segment, as the forward pass left it, needs no recompute
         if (!(tail_ok && hi == L - 1)) {
+            std::vector<StepBufs> plan;
+            PCData* cur = S[0];
             for (int j = 0; j < cnt - 1; ++j) {
                 PCData* out = (j + 1 < cnt - 1) ? S[j + 1] : G.ping.get();
-                step_forward<R>(c, *S[j], *out, G.sgrid[j], G.strust[j], s);
+                plan.push_back({cur, out, &G.sgrid[j], &G.strust[j]});
+                cur = out;
             }
+            run_forward_steps<R>(c, plan, s);
         }
         const int stop = std::max(control, lo);
         for (int i = hi - 1; i >= stop; --i) {
@@ -1488,6 +1564,14 @@ int mpm_set_scatter_mode(int mode)
     return guard([&] {
         if (mode != 0 && mode != 1) fail(MPM_ERR_ARG, "scatter mode must be 0 or 1");
         g_scatter_mode = mode;
+    });
+}
+
+int mpm_set_fused_steps(int on)
+{
+    return guard([&] {
+        if (on != 0 && on != 1) fail(MPM_ERR_ARG, "fused steps must be 0 or 1");
+        g_fuse_steps = on;
     });
 }
 

@@ -35,9 +35,17 @@ namespace mpm {
 #ifndef MPM_G2P_MIN_BLOCKS
 #define MPM_G2P_MIN_BLOCKS 3
 #endif
+#ifndef MPM_G2P2G_MIN_BLOCKS
+#define MPM_G2P2G_MIN_BLOCKS 3
+#endif
+// G2P of a step fused with the next step's P2G (FP32, segmented scatter)
+#ifndef MPM_FUSE_G2P2G
+#define MPM_FUSE_G2P2G 1
+#endif
 
 int g_tile_nodes = 2048;
 int g_scatter_mode = 1;
+int g_fuse_steps = 1;
 long long g_launches = 0;
 
 namespace {
@@ -1034,6 +1042,58 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<flo
     }
 }
 
+// G2P of step i fused with P2G of step i+1 (FP32, segmented scatter).  The
+// state G2P forms for layer i+1 -- stored as usual for the tape -- stays in
+// registers and feeds the next step's stress and scatter, so that step does
+// not read it back; layer i+1 has no control (a forward pass zeroes the
+// control of every layer it writes, ForwardSimulation.cpp:155).  grid is
+// step i's updated grid (read); grid1 is step i+1's, zeroed (scattered into).
+template <int K>
+__global__ void __launch_bounds__(kThreads, MPM_G2P2G_MIN_BLOCKS)
+k_g2p2g(KP<float> kp, int n, long long ld, const float* __restrict__ st, const float* __restrict__ dfc,
+        const float* __restrict__ co, const float* __restrict__ grid, float* __restrict__ st1,
+        float* __restrict__ trust, float* __restrict__ grid1, int tile_cap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    long long goff;
+    bind_instance(kp, n, goff);
+    grid += goff * 4;
+    grid1 += goff * 4;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = p < n;
+    Stencil<float, K> sten;
+    float A[9], mv[3], mass = 0.f;
+    if (valid) {
+        float x1[3], vs[3] = {0.f, 0.f, 0.f}, C1[9], F1[9];
+        {
+            float x[3], F[9], Ft[9];
+            load_planes(st + ST_X * ld, ld, p, 3, x);
+            load_Ft(st, dfc, ld, p, F, Ft);
+            Stencil<float, K> sn;
+            make_stencil<float, K>(x, kp.gmin, kp.dx, kp.inv_dx, sn, false);
+            float Cx[3] = {0, 0, 0}, Cy[3] = {0, 0, 0}, Cz[3] = {0, 0, 0};
+            if (stencil_inside(kp, sn)) g2p_gather<float, K, false>(kp, sn, grid, vs, Cx, Cy, Cz);
+            else g2p_gather<float, K, true>(kp, sn, grid, vs, Cx, Cy, Cz);
+            g2p_finish(kp, ld, p, x, F, Ft, vs, Cx, Cy, Cz, st1, trust, x1, C1, F1);
+        }
+        mass = co[CO_M * ld + p];
+        const float vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
+        Inv<float> iv;
+        invariants(F1, iv);
+        float P[9], Rm[9], S[9], PF[9];
+        pk(kp.material, F1, lam, mu, iv, P, Rm, S);
+        mulNT3(P, F1, PF);
+        const float trC = C1[0] + C1[4] + C1[8];
+        const float k1 = -kp.C0 * kp.dt * vol;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = k1 * (PF[i] + ((i % 4 == 0) ? kp.bulk * trC : 0.f)) + mass * C1[i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) mv[a] = mass * vs[a] * kp.dragf;
+        make_stencil<float, K>(x1, kp.gmin, kp.dx, kp.inv_dx, sten, false);
+    }
+    seg_scatter<K, 4>(kp, valid, sten, mv, mass, A, grid1, tile_cap, smem);
+}
+
 // Deterministic mode: the node sums of P2G (fixed point) -> mass clamp +
 // G_op, as k_grid_update; clears the accumulators for the next step
 __global__ void k_grid_update_fix(KP<float> kp, long long nn, FixArgs fx, float* __restrict__ grid)
@@ -1962,6 +2022,35 @@ void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc
     counted();
     if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
     else k_p2g<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+}
+
+bool g2p2g_applies(const StepCfg& c, int prec_bytes)
+{
+#if MPM_FUSE_G2P2G
+    return prec_bytes == 4 && c.fuse && !c.det() && scatter_mode_of(c) == 1;
+#else
+    (void)c;
+    (void)prec_bytes;
+    return false;
+#endif
+}
+
+void launch_g2p2g(const StepCfg& c, int n, long long ld, const float* st, const float* dfc, const float* co,
+                  const float* grid, float* st1, float* trust, float* grid1, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const int cap = tile_cap_for<float>(c);
+    auto kp = make_kp<float>(c);
+    const size_t sm = seg_smem_bytes(kThreads, cap, 4);
+    if (c.kernel == 0) {
+        ensure_smem(k_g2p2g<4>, sm);
+        counted();
+        k_g2p2g<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
+    } else {
+        ensure_smem(k_g2p2g<3>, sm);
+        counted();
+        k_g2p2g<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
+    }
 }
 
 template <typename R>

@@ -41,6 +41,9 @@ struct StepCfg {
     int scatter_mode = -1;
     int adj_tile_nodes = -1;
     int gather_tile_nodes = -1;
+    // 1: a run of forward steps fuses each G2P with the next step's P2G
+    // where the configuration allows it (g2p2g_applies); 0: step by step
+    int fuse = 1;
     // Deterministic scatters (FP32 segmented path): node sums accumulate in
     // 64-bit fixed point, so their value does not depend on the order of the
     // atomics.  fix: 4 words per node, all zero between steps (the grid
@@ -80,6 +83,8 @@ extern int g_tile_nodes;
 // FP32 scatter strategy: 1 = segmented (warp per cell segment, lane per
 // node), 0 = per-particle scatter
 extern int g_scatter_mode;
+// fused G2P -> next P2G in forward passes (1, the default) or not (0)
+extern int g_fuse_steps;
 // kernels launched by the launchers below (host-side count)
 extern long long g_launches;
 
@@ -91,6 +96,13 @@ void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s);
 template <typename R>
 void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* grid, R* st1, R* trust,
                 cudaStream_t s);
+// G2P of step i fused with P2G of step i+1 (FP32 segmented scatter, not
+// deterministic): reads step i's updated grid, writes layer i+1 (st1, trust)
+// and scatters layer i+1 into grid1 (zeroed).  g2p2g_applies: whether the
+// configuration (precision, deterministic mode, scatter strategy) uses it.
+bool g2p2g_applies(const StepCfg& c, int prec_bytes);
+void launch_g2p2g(const StepCfg& c, int n, long long ld, const float* st, const float* dfc, const float* co,
+                  const float* grid, float* st1, float* trust, float* grid1, cudaStream_t s);
 // adjoint: G2P^T scatter (+P_op_2^T), grid update^T, P2G^T gather (+P_op_1^T)
 template <typename R>
 void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* st1, const R* g1,

@@ -61,6 +61,7 @@ _SIGS = {
     "mpm_set_verbose": [C.c_int],
     "mpm_set_tile_nodes": [C.c_int],
     "mpm_set_scatter_mode": [C.c_int],
+    "mpm_set_fused_steps": [C.c_int],
     "mpm_lame": [C.c_double, C.c_double, _dp, _dp],
     "mpm_pointcloud_create": [C.c_int, C.c_int, C.POINTER(_vp)],
     "mpm_pointcloud_set": [_vp, C.c_int, _vp, C.c_int, C.c_int],

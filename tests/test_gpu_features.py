@@ -335,15 +335,19 @@ def test_profiler_counts_graph_replays(dm):
     try:
         for _ in range(4):  # eager, record, replay, replay
             cg.compute_forward_pass(0, 0)
-        cnt, ms = C.c_longlong(), C.c_double()
+        cnt, ms, cnt2, ms2 = C.c_longlong(), C.c_double(), C.c_longlong(), C.c_double()
         lib.mpm_profile_query(0, C.byref(cnt), C.byref(ms))  # p2g
+        lib.mpm_profile_query(10, C.byref(cnt2), C.byref(ms2))  # g2p2g: G2P fused with the next P2G
     finally:
         lib.mpm_profile_enable(0)
-    assert cnt.value == 4 * T and ms.value > 0
-    # the launch counter counts kernels: P2G, grid update, G2P per step
+    # every step's P2G ran once per pass: the first on its own, the others
+    # inside the fused G2P -> P2G kernel
+    assert cnt.value == 4 and cnt2.value == 4 * (T - 1) and ms.value > 0 and ms2.value > 0
+    # the launch counter counts kernels: P2G, then per step the grid update
+    # and the fused kernel (plain G2P for the last step)
     n0 = lib.mpm_launch_count()
     cg.compute_forward_pass(0, 0)
-    assert lib.mpm_launch_count() - n0 == 3 * T
+    assert lib.mpm_launch_count() - n0 == 2 * T + 1
 
 
 def test_autotune_picks_a_valid_configuration(dm, orc):
@@ -418,3 +422,27 @@ def test_nonfinite_state_is_flagged_not_fatal(dm):
     cg.get_point_cloud(0).set("v", v)
     cg.compute_forward_pass(0, 0)
     assert not cg.has_nonfinite(T)
+
+
+@pytest.mark.parametrize("checkpoint_every", [1, 5])
+def test_fused_forward_steps_agree_with_step_by_step(dm, orc, checkpoint_every):
+    """Forward passes run each step's G2P fused with the next step's P2G
+    (k_g2p2g): the same computation as the three kernels step by step, so
+    the two agree to the order of the float atomics, and both match the
+    oracle; full tape and checkpointed (where the scratch grids alternate)."""
+    s0, g, rng, _, _ = _case(6, G=16, smoothing=0.1, drag=0.2)
+    prm = O.Params(dt=1e-3, drag=0.2, smoothing=0.1, exact=True)
+    T = 12
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    lib = dm._lib.lib
+    xf, gf, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, "fp32", checkpoint_every=checkpoint_every)
+    try:
+        assert lib.mpm_set_fused_steps(0) == 0
+        xs, gs, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, "fp32", checkpoint_every=checkpoint_every)
+    finally:
+        lib.mpm_set_fused_steps(1)
+    xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    assert rel_err(xf, xs) < 1e-6 and rel_err(xf, xw) < 1e-6
+    for k, want in (("x", gw.x), ("v", gw.v), ("F", gw.F), ("C", gw.C), ("dFc", gw.Ft)):
+        assert norm_err(gf[k], gs[k]) < 1e-5, k
+        assert norm_err(gf[k], want) < 2e-4, k
