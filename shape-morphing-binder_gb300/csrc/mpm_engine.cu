@@ -2164,7 +2164,14 @@ int mpm_compgraph_active_nodes(mpm_compgraph* cg, int layer, unsigned long long*
         check_cg(cg);
         Graph& G = cg->g;
         if (layer < 0 || layer >= (int)G.layers.size()) fail(MPM_ERR_RANGE, "layer %d out of range", layer);
-        const Buf& gb = G.layers[layer].grid ? G.layers[layer].grid : G.fgrid;
+        // the layer's own grid (full tape), else a scratch grid of the last
+        // forward pass of a checkpointed graph
+        const Buf* pick = &G.layers[layer].grid;
+        for (const Buf* cand : {&G.fgrid, &G.fgrid2})
+            if (!*pick) pick = cand;
+        for (const Buf& cand : G.sgrid)
+            if (!*pick) pick = &cand;
+        const Buf& gb = *pick;
         if (!gb) fail(MPM_ERR_STATE, "layer %d has no forward grid", layer);
         DevBuf d(sizeof(unsigned long long));
         StepCfg c = G.cfg();
