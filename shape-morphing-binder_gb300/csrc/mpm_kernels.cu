@@ -315,7 +315,7 @@ MPM_D void walk_rotated(const Stencil<R, K>& st, Fn&& f)
 // of particle p to node n is  w_pn * [u0_p + A_p dg_pn, (m_p)].
 // ------------------------------------------------------------------------
 
-constexpr int kRec = 40;  // u0[3], m, A[9], pad[3], w[3][K<=4], g[3][K<=4]
+constexpr int kRec = 40;  // u0[3], m, A[9], pad[3], (w, g) pairs [3][K<=4]
 
 inline size_t seg_smem_bytes(int CH, int tile_cap, int NC, bool det = false)
 {
@@ -399,8 +399,8 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int o = 0; o < K; ++o) {
-                r[16 + a * K + o] = st.w[a][o];
-                r[28 + a * K + o] = st.g[a][o];
+                r[16 + 2 * (a * K + o)] = st.w[a][o];
+                r[17 + 2 * (a * K + o)] = st.g[a][o];
             }
     }
     __syncthreads();
@@ -472,21 +472,26 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
                 const float4 qa = *reinterpret_cast<const float4*>(r + 4);
                 const float4 qb = *reinterpret_cast<const float4*>(r + 8);
                 const float a8 = r[12];
-                const float wyz = r[16 + K + bb] * r[16 + 2 * K + cc];
-                const float gy = r[28 + K + bb], gz = r[28 + 2 * K + cc];
+                // (w, g) of the lane's y and z stencil offsets: one 8-byte load each
+                const float2 wgy = *reinterpret_cast<const float2*>(r + 16 + 2 * (K + bb));
+                const float2 wgz = *reinterpret_cast<const float2*>(r + 16 + 2 * (2 * K + cc));
+                const float wyz = wgy.x * wgz.x;
+                const float gy = wgy.y, gz = wgz.y;
                 // A row-major: (qa.x qa.y qa.z | qa.w qb.x qb.y | qb.z qb.w a8)
                 const float c0 = q0.x + qa.y * gy + qa.z * gz;
                 const float c1 = q0.y + qb.x * gy + qb.y * gz;
                 const float c2 = q0.z + qb.w * gy + a8 * gz;
                 {
-                    const float w = r[16 + a0] * wyz, gx = r[28 + a0];
+                    const float2 wgx = *reinterpret_cast<const float2*>(r + 16 + 2 * a0);
+                    const float w = wgx.x * wyz, gx = wgx.y;
                     acc0[0] += w * (c0 + qa.x * gx);
                     acc0[1] += w * (c1 + qa.w * gx);
                     acc0[2] += w * (c2 + qb.z * gx);
                     if (NC == 4) acc0[NC - 1] += w * q0.w;
                 }
                 if (has1) {
-                    const float w = r[16 + a1] * wyz, gx = r[28 + a1];
+                    const float2 wgx = *reinterpret_cast<const float2*>(r + 16 + 2 * a1);
+                    const float w = wgx.x * wyz, gx = wgx.y;
                     acc1[0] += w * (c0 + qa.x * gx);
                     acc1[1] += w * (c1 + qa.w * gx);
                     acc1[2] += w * (c2 + qb.z * gx);
