@@ -149,14 +149,33 @@ KERNEL_BYTES = {
 def build_graph(dm, w, precision, checkpoint, adjoint="exact", deterministic=False):
     kernel, material = w.extra.get("kernel", "cubic"), w.extra.get("material", "fcr")
     dt = np.float64 if precision == "fp64" else np.float32
+    Cm = w.extra.get("C")
     pc = dm.PointCloud.from_arrays(w.x.astype(dt), v=w.v.astype(dt), F=w.F.astype(dt), m=w.m.astype(dt),
                                    vol=w.vol.astype(dt), lam=w.lam.astype(dt), mu=w.mu.astype(dt),
-                                   precision=precision)
+                                   C_=None if Cm is None else Cm.astype(dt), precision=precision)
     grid = dm.Grid(*w.dims, w.dx, w.grid_min, precision=precision)
     cg = dm.CompGraph(pc, grid, grid, adjoint=adjoint, checkpoint_every=checkpoint, deterministic=deterministic,
                       kernel=kernel, material=material)
     cg.set_sim_params(dt=w.dt, drag=w.drag, smoothing=w.smoothing)
     return cg, (pc, grid)
+
+
+def advance_workload(dm, w, steps):
+    """The workload's state after `steps` forward steps (FP32), in the
+    caller's particle order: the particles have drifted away from the cell
+    order of the input, as they have late in a long rollout.  With the
+    set-up re-sort (the default) the timed graph starts re-sorted, with
+    --no-resort it keeps the drifted order: the pair measures what a re-sort
+    at a stored layer would buy."""
+    cg, keep = build_graph(dm, w, "fp32", w.checkpoint)
+    cg.set_up_comp_graph(steps + 1)
+    cg.compute_forward_pass(0, 0)
+    last = cg.get_point_cloud(steps)
+    w.x, w.v, w.F = last.get("x", np.float64), last.get("v", np.float64), last.get("F", np.float64)
+    w.extra["C"] = last.get("C", np.float64)
+    w.extra["advanced_steps"] = steps
+    del cg, keep
+    return w
 
 
 def device_rollout(torch, cg, T, tgt, n):
@@ -219,6 +238,8 @@ def run_ours(args, rank, world, device):
         args.no_e2e, args.no_fp64, args.no_cpu = True, True, True
     else:
         w = make_workload(args.workload, args.quick, args.timesteps, args.checkpoint)
+        if args.from_rollout:
+            w = advance_workload(dm, w, args.from_rollout)
         if args.shuffle:
             p = np.random.default_rng(5).permutation(w.n)
             for k in ("x", "v", "F", "m", "vol", "lam", "mu", "target"):
@@ -328,6 +349,7 @@ def run_ours(args, rank, world, device):
                    "bench_step": "one rollout: forward T steps + loss gradient + backward T steps",
                    "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic),
                    "particle_order": ("shuffled" if args.shuffle else "cell-sorted input") +
+                                     (f", advanced {args.from_rollout} steps (drifted)" if args.from_rollout else "") +
                                      ("" if args.no_resort else ", re-sorted by cell at set-up"),
                    "gradients": "layer 0: x, v, F, C, control F" + (", lam, mu (dL/dE)" if w.extra.get("grad_E")
                                                                     else "")},
@@ -492,7 +514,7 @@ def run_e2e(torch, dm, args, w, device, keep, tuning=None):
         cg.enable_lame_grads(True)
     if tuning:  # the device arm's kernel configuration
         cg.set_tuning(tuning["tile_nodes"], tuning["scatter_mode"], tuning.get("adj_tile_nodes", -1),
-                      tuning.get("gather_tile_nodes", -1))
+                      tuning.get("gather_tile_nodes", -1), tuning.get("block_threads", -1))
     cg.set_up_comp_graph(T + 1)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).pin_memory()  # noqa: E731
     hx, hv, hF = pin(w.x), pin(w.v), pin(w.F)
@@ -766,6 +788,8 @@ def main():
     ap.add_argument("--no-det", action="store_true", help="morph500k: float atomics instead of fixed point")
     ap.add_argument("--shuffle", action="store_true", help="shuffle the particle order of the workload")
     ap.add_argument("--no-resort", action="store_true", help="keep the input particle order (no cell re-sort)")
+    ap.add_argument("--from-rollout", type=int, default=0,
+                    help="start from the state after this many forward steps (drifted particle order)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
