@@ -300,14 +300,23 @@ int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scat
  * (-1: follow the set_tuning budget, the default; 0..2816 nodes); get
  * returns the budgets in effect */
 int mpm_compgraph_set_adjoint_tiles(mpm_compgraph* cg, int scatter_nodes, int gather_nodes);
+/* No counterpart in the reference: threads per block of the step kernels
+ * (P2G, the fused G2P->P2G, G2P and the two adjoint kernels), 128 or 256
+ * (-1: 256, the default).  Each thread takes one particle, so this is also
+ * the particles per block; the segmented scatter's node tile covers one
+ * block's particles. */
+int mpm_compgraph_set_block_threads(mpm_compgraph* cg, int threads);
+int mpm_compgraph_get_block_threads(const mpm_compgraph* cg, int* threads);
 int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes, int* gather_nodes);
 /* No counterpart in the reference: time `steps`-step forward+backward passes
  * of a scratch copy of this graph (layer 0's state) for each candidate
  * scatter strategy and P2G tile budget, then for each budget of the G2P
- * transpose's scatter tile and of the P2G transpose's gather tile (one at a
- * time, the others held), keep the fastest for this graph and return P2G's
+ * transpose's scatter tile and of the P2G transpose's gather tile, then for
+ * 128 against 256 threads (and particles) per block (one knob at a time,
+ * the others held), keep the fastest for this graph and return P2G's
  * choice (best_ms: one timed forward+backward of the winner; the adjoint
- * budgets: mpm_compgraph_get_adjoint_tiles) */
+ * budgets: mpm_compgraph_get_adjoint_tiles; the block size:
+ * mpm_compgraph_get_block_threads) */
 int mpm_compgraph_autotune(mpm_compgraph* cg, int steps, int* best_tile, int* best_mode, double* best_ms);
 /* the same, timing the candidates from the state of `layer` (a stored layer
  * after a forward pass).  A layer deep in a rollout has drifted from the

@@ -568,6 +568,7 @@ struct Graph {
     std::map<std::string, std::unique_ptr<Cap>> caps;
     bool graphs_on = true;
     int tile_nodes = -1, scatter_mode = -1;  // tuning (-1: library defaults)
+    int block_threads = -1;  // threads per block of the step kernels (-1: 256)
     int adj_tile_nodes = -1;                 // G2P-transpose scatter tile (-1: tile_nodes)
     int gather_tile_nodes = -1;              // P2G-transpose gather tile (-1: tile_nodes)
     // deterministic scatters (opt.deterministic): fixed-point node
@@ -607,6 +608,7 @@ struct Graph {
         c.tile_nodes = tile_nodes;
         c.scatter_mode = scatter_mode;
         c.fuse = g_fuse_steps;
+        c.threads = block_threads > 0 ? block_threads : 256;
         c.adj_tile_nodes = adj_tile_nodes;
         c.gather_tile_nodes = gather_tile_nodes;
         double max_dx = geom.dx;
@@ -2262,6 +2264,23 @@ int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scat
     });
 }
 
+int mpm_compgraph_set_block_threads(mpm_compgraph* cg, int threads)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (threads != -1 && threads != 128 && threads != 256) fail(MPM_ERR_ARG, "block threads must be -1, 128 or 256");
+        cg->g.block_threads = threads;
+    });
+}
+
+int mpm_compgraph_get_block_threads(const mpm_compgraph* cg, int* threads)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (threads) *threads = cg->g.block_threads > 0 ? cg->g.block_threads : 256;
+    });
+}
+
 int mpm_compgraph_set_adjoint_tiles(mpm_compgraph* cg, int scatter_nodes, int gather_nodes)
 {
     return guard([&] {
@@ -2316,7 +2335,7 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
         const int adj_tiles[] = {512, 1024, 2048};
         const int gather_tiles[] = {1024, 2048, 2816};
         double best = 1e300;
-        int bt = -1, bm = -1, ba = -1, bg = -1;
+        int bt = -1, bm = -1, ba = -1, bg = -1, bth = 256;
         cudaEvent_t e0, e1;
         ck(cudaEventCreate(&e0), "event");
         ck(cudaEventCreate(&e1), "event");
@@ -2375,6 +2394,14 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
                 ba = sweep(adj_tiles, 3, T.adj_tile_nodes, 1024);
                 bg = sweep(gather_tiles, 3, T.gather_tile_nodes, 2048);
             }
+            // 4. threads (= particles) per block of the step kernels
+            T.block_threads = 128;
+            const double ms128 = time_pass();
+            if (ms128 < best) {
+                best = ms128;
+                bth = 128;
+            }
+            T.block_threads = bth;
         });
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
@@ -2382,6 +2409,7 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
         G.scatter_mode = bm;
         G.adj_tile_nodes = ba;
         G.gather_tile_nodes = bg;
+        G.block_threads = bth;
         if (best_tile) *best_tile = bt;
         if (best_mode) *best_mode = bm;
         if (best_ms) *best_ms = best;

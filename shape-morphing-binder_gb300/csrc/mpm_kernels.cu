@@ -1990,43 +1990,44 @@ template <typename R>
 void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
                 cudaStream_t s)
 {
+    const int T = c.threads == 128 ? 128 : kThreads;
     if (n <= 0) return;
     const int cap = tile_cap_for<R>(c);
     auto kp = make_kp<R>(c);
     if constexpr (sizeof(R) == 4) {
         if (c.det()) {
             const FixArgs fx = make_fix(c);
-            const size_t sm = seg_smem_bytes(kThreads, cap, 4, true);
+            const size_t sm = seg_smem_bytes(T, cap, 4, true);
             if (c.kernel == 0) {
                 ensure_smem(k_p2g_seg<4, true>, sm);
                 counted();
-                k_p2g_seg<4, true><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+                k_p2g_seg<4, true><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             } else {
                 ensure_smem(k_p2g_seg<3, true>, sm);
                 counted();
-                k_p2g_seg<3, true><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+                k_p2g_seg<3, true><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             }
             return;
         }
         if (scatter_mode_of(c) == 1) {
-            const size_t sm = seg_smem_bytes(kThreads, cap, 4);
+            const size_t sm = seg_smem_bytes(T, cap, 4);
             const FixArgs fx{};
             if (c.kernel == 0) {
                 ensure_smem(k_p2g_seg<4, false>, sm);
                 counted();
-                k_p2g_seg<4, false><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+                k_p2g_seg<4, false><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             } else {
                 ensure_smem(k_p2g_seg<3, false>, sm);
                 counted();
-                k_p2g_seg<3, false><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
+                k_p2g_seg<3, false><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap, fx);
             }
             return;
         }
     }
     const size_t sm = (size_t)cap * 4 * sizeof(R);
     counted();
-    if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
-    else k_p2g<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+    if (c.kernel == 0) k_p2g<R, 4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
+    else k_p2g<R, 3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, cap);
 }
 
 bool g2p2g_applies(const StepCfg& c, int prec_bytes)
@@ -2043,18 +2044,19 @@ bool g2p2g_applies(const StepCfg& c, int prec_bytes)
 void launch_g2p2g(const StepCfg& c, int n, long long ld, const float* st, const float* dfc, const float* co,
                   const float* grid, float* st1, float* trust, float* grid1, cudaStream_t s)
 {
+    const int T = c.threads == 128 ? 128 : kThreads;
     if (n <= 0) return;
     const int cap = tile_cap_for<float>(c);
     auto kp = make_kp<float>(c);
-    const size_t sm = seg_smem_bytes(kThreads, cap, 4);
+    const size_t sm = seg_smem_bytes(T, cap, 4);
     if (c.kernel == 0) {
         ensure_smem(k_g2p2g<4>, sm);
         counted();
-        k_g2p2g<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
+        k_g2p2g<4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
     } else {
         ensure_smem(k_g2p2g<3>, sm);
         counted();
-        k_g2p2g<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
+        k_g2p2g<3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, grid, st1, trust, grid1, cap);
     }
 }
 
@@ -2077,17 +2079,19 @@ template <typename R>
 void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* grid, R* st1, R* trust,
                 cudaStream_t s)
 {
+    const int T = c.threads == 128 ? 128 : kThreads;
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
     counted();
-    if (c.kernel == 0) k_g2p<R, 4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
-    else k_g2p<R, 3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
+    if (c.kernel == 0) k_g2p<R, 4><<<nblocks(n, T), T, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
+    else k_g2p<R, 3><<<nblocks(n, T), T, 0, s>>>(kp, n, ld, st, dfc, grid, st1, trust);
 }
 
 template <typename R>
 void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* st1, const R* g1,
                     const R* trust, R* adj, cudaStream_t s)
 {
+    const int T = c.threads == 128 ? 128 : kThreads;
     if (n <= 0) return;
     const int cap = adj_cap_for<R>(c);
     auto kp = make_kp<R>(c);
@@ -2096,40 +2100,40 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
             // inputs of the scatter and their bound first, then the scatter
             const FixArgs fx = make_fix(c);
             cudaMemsetAsync(c.fix_ctl + 1, 0, 2 * sizeof(unsigned), s);
-            const size_t sm = seg_smem_bytes(kThreads, cap, 3, true);
+            const size_t sm = seg_smem_bytes(T, cap, 3, true);
             if (c.kernel == 0) {
                 counted();
-                k_g2p_adj_prep<4><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
+                k_g2p_adj_prep<4><<<nblocks(n, T), T, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
                 ensure_smem(k_g2p_adj_fix<4>, sm);
                 counted();
-                k_g2p_adj_fix<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
+                k_g2p_adj_fix<4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
             } else {
                 counted();
-                k_g2p_adj_prep<3><<<nblocks(n), kThreads, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
+                k_g2p_adj_prep<3><<<nblocks(n, T), T, 0, s>>>(kp, n, ld, st, dfc, st1, g1, trust, fx, c.fix_scr);
                 ensure_smem(k_g2p_adj_fix<3>, sm);
                 counted();
-                k_g2p_adj_fix<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
+                k_g2p_adj_fix<3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, c.fix_scr, fx, cap);
             }
             return;
         }
         if (scatter_mode_of(c) == 1) {
-            const size_t sm = seg_smem_bytes(kThreads, cap, 3);
+            const size_t sm = seg_smem_bytes(T, cap, 3);
             if (c.kernel == 0) {
                 ensure_smem(k_g2p_adj_seg<4>, sm);
                 counted();
-                k_g2p_adj_seg<4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+                k_g2p_adj_seg<4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             } else {
                 ensure_smem(k_g2p_adj_seg<3>, sm);
                 counted();
-                k_g2p_adj_seg<3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+                k_g2p_adj_seg<3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
             }
             return;
         }
     }
     const size_t sm = (size_t)cap * 3 * sizeof(R);
     counted();
-    if (c.kernel == 0) k_g2p_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
-    else k_g2p_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+    if (c.kernel == 0) k_g2p_adj<R, 4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
+    else k_g2p_adj<R, 3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, st1, g1, trust, adj, cap);
 }
 
 template <typename R>
@@ -2152,6 +2156,7 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
                     const R* g1, const R* trust, const R* grid, const R* adj, R* g, R* gFt, R* glam, R* gmu,
                     cudaStream_t s)
 {
+    const int T = c.threads == 128 ? 128 : kThreads;
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
     const int cap = gather_cap_for<R>(c);
@@ -2159,12 +2164,12 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
     if (c.kernel == 0) {
         ensure_smem(k_p2g_adj<R, 4>, sm);
         counted();
-        k_p2g_adj<R, 4><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+        k_p2g_adj<R, 4><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
                                                           glam, gmu, cap);
     } else {
         ensure_smem(k_p2g_adj<R, 3>, sm);
         counted();
-        k_p2g_adj<R, 3><<<nblocks(n), kThreads, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
+        k_p2g_adj<R, 3><<<nblocks(n, T), T, sm, s>>>(kp, n, ld, st, dfc, co, st1, g1, trust, grid, adj, g, gFt,
                                                           glam, gmu, cap);
     }
 }

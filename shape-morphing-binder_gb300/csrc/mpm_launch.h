@@ -44,6 +44,9 @@ struct StepCfg {
     // 1: a run of forward steps fuses each G2P with the next step's P2G
     // where the configuration allows it (g2p2g_applies); 0: step by step
     int fuse = 1;
+    // threads (= particles) per block of the particle kernels of a step:
+    // 256 or 128
+    int threads = 256;
     // Deterministic scatters (FP32 segmented path): node sums accumulate in
     // 64-bit fixed point, so their value does not depend on the order of the
     // atomics.  fix: 4 words per node, all zero between steps (the grid

@@ -414,8 +414,8 @@ class CompGraph:
         check(lib.mpm_compgraph_set_stream(self._h, C.c_void_p(ptr) if ptr else None))
 
     def autotune(self, steps: int = 4, layer: int = 0) -> dict:
-        """Pick the fastest scatter strategy and node-tile budgets for this
-        graph by timing short forward+backward passes from the state of
+        """Pick the fastest scatter strategy, node-tile budgets and block size
+        for this graph by timing short forward+backward passes from the state of
         `layer` (additive; a stored layer deep in a computed rollout reflects
         the particle drift of long rollouts)."""
         t, m, ms = C.c_int(), C.c_int(), C.c_double()
@@ -425,19 +425,23 @@ class CompGraph:
         out.update(ms_per_pass=ms.value, steps=int(steps), from_layer=int(layer))
         return out
 
-    def set_tuning(self, tile_nodes=-1, scatter_mode=-1, adj_tile_nodes=-1, gather_tile_nodes=-1):
-        """P2G's tile budget and the scatter strategy, and the tile budgets of
-        the G2P transpose's scatter and the P2G transpose's gather (-1:
-        library defaults; the adjoint budgets follow P2G's)."""
+    def set_tuning(self, tile_nodes=-1, scatter_mode=-1, adj_tile_nodes=-1, gather_tile_nodes=-1,
+                   block_threads=-1):
+        """P2G's tile budget and the scatter strategy, the tile budgets of
+        the G2P transpose's scatter and the P2G transpose's gather, and the
+        threads (= particles) per block of the step kernels (-1: library
+        defaults; the adjoint budgets follow P2G's; 256 threads)."""
         check(lib.mpm_compgraph_set_tuning(self._h, int(tile_nodes), int(scatter_mode)))
         check(lib.mpm_compgraph_set_adjoint_tiles(self._h, int(adj_tile_nodes), int(gather_tile_nodes)))
+        check(lib.mpm_compgraph_set_block_threads(self._h, int(block_threads)))
 
     def get_tuning(self) -> dict:
-        t, m, at, gt = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        t, m, at, gt, th = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(lib.mpm_compgraph_get_tuning(self._h, C.byref(t), C.byref(m)))
         check(lib.mpm_compgraph_get_adjoint_tiles(self._h, C.byref(at), C.byref(gt)))
+        check(lib.mpm_compgraph_get_block_threads(self._h, C.byref(th)))
         return {"tile_nodes": t.value, "scatter_mode": m.value, "adj_tile_nodes": at.value,
-                "gather_tile_nodes": gt.value}
+                "gather_tile_nodes": gt.value, "block_threads": th.value}
 
     def use_graphs(self, on=True):
         """Replay forward/backward passes as CUDA graphs (default on)."""

@@ -120,6 +120,8 @@ _SIGS = {
     "mpm_compgraph_autotune_from": [_vp, C.c_int, C.c_int, _ip, _ip, _dp],
     "mpm_compgraph_set_adjoint_tiles": [_vp, C.c_int, C.c_int],
     "mpm_compgraph_get_adjoint_tiles": [_vp, _ip, _ip],
+    "mpm_compgraph_set_block_threads": [_vp, C.c_int],
+    "mpm_compgraph_get_block_threads": [_vp, _ip],
     "mpm_compgraph_synchronize": [_vp],
     "mpm_profile_enable": [C.c_int],
     "mpm_profile_reset": [],

@@ -357,8 +357,9 @@ def test_autotune_picks_a_valid_configuration(dm, orc):
     res = cg.autotune(steps=2)
     assert res["tile_nodes"] in (0, 512, 1024, 2048) and res["scatter_mode"] in (0, 1) and res["ms_per_pass"] > 0
     assert res["adj_tile_nodes"] in (512, 1024, 2048) and res["gather_tile_nodes"] in (1024, 2048, 2816)
+    assert res["block_threads"] in (128, 256)
     assert cg.get_tuning() == {k: res[k] for k in ("tile_nodes", "scatter_mode", "adj_tile_nodes",
-                                                   "gather_tile_nodes")}
+                                                   "gather_tile_nodes", "block_threads")}
     cg.compute_forward_pass(0, 0)
     want, _ = orc.forward_step(g, prm, s0)
     assert rel_err(cg.get_point_cloud(1).get("x", np.float64), want.x) < 1e-6
@@ -446,3 +447,34 @@ def test_fused_forward_steps_agree_with_step_by_step(dm, orc, checkpoint_every):
     for k, want in (("x", gw.x), ("v", gw.v), ("F", gw.F), ("C", gw.C), ("dFc", gw.Ft)):
         assert norm_err(gf[k], gs[k]) < 1e-5, k
         assert norm_err(gf[k], want) < 2e-4, k
+
+
+@pytest.mark.parametrize("deterministic", [False, True])
+def test_block_threads_128_matches_256(dm, orc, deterministic):
+    """The step kernels at 128 threads (and particles) per block give the
+    same results as at 256 (bit for bit with the fixed-point scatters) and
+    match the oracle."""
+    s0, g, rng, _, _ = _case(8, G=14, smoothing=0.1, drag=0.2)
+    prm = O.Params(dt=1e-3, drag=0.2, smoothing=0.1, exact=True)
+    T = 6
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    out = {}
+    for threads in (256, 128):
+        cg, keep = make_graph(dm, s0, g, prm, precision="fp32", adjoint="exact", layers=T + 1, checkpoint_every=3,
+                              deterministic=deterministic)
+        cg.set_tuning(block_threads=threads)
+        assert cg.get_tuning()["block_threads"] == threads
+        cg.compute_forward_pass(0, 0)
+        last = cg.get_point_cloud(T)
+        last.set("grad_x", seed_gx)
+        cg.compute_backward_pass(0)
+        out[threads] = (last.get("x", np.float64), get_grads(cg, 0), cg.get_grad(0, "dFc", np.float64))
+    xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    (xa, ga, ca), (xb, gb, cb) = out[256], out[128]
+    if deterministic:
+        assert np.array_equal(xa, xb) and np.array_equal(ca, cb)
+        for k in ga:
+            assert np.array_equal(ga[k], gb[k]), k
+    assert rel_err(xb, xw) < 1e-6 and norm_err(cb, gw.Ft) < 2e-4
+    for k, want in (("x", gw.x), ("v", gw.v), ("F", gw.F), ("C", gw.C)):
+        assert norm_err(gb[k], want) < 2e-4, k
