@@ -303,8 +303,10 @@ MPM_HD void sym_eig3(const double* Ain, double* w, double* V)
 }
 
 // Rotation-variant polar factor through an SVD (double): R = U V^T, det R = +1,
-// the sign of det F carried by the smallest singular value.
-MPM_HD void polar_svd(const double* F, double* Rm)
+// the sign of det F carried by the smallest singular value.  Out of line: it
+// runs only for F near inversion (the FP64 guard), and keeping its code out
+// of the step kernels lets the P2G transpose run 2% faster.
+static __host__ __device__ __noinline__ void polar_svd(const double* F, double* Rm)
 {
     double FtF[9], w[3], V[9];
     mulTN3(F, F, FtF);
