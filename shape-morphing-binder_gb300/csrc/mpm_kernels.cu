@@ -373,6 +373,16 @@ MPM_D unsigned long long to_fix(float y, float scale, bool& ovf)
     return (unsigned long long)__float2ll_rn(z);
 }
 
+// Adds NC channel sums to a 16-byte grid node as one vector reduction
+// (sm_90+).  With 3 channels (the adjoint grid's dL/dv, zeroed before the
+// scatter) the fourth lane adds zero to a channel the scatter leaves free.
+template <int NC>
+MPM_D void add_node(float* node, const float* v)
+{
+    static_assert(NC == 3 || NC == 4, "grid nodes hold 4 floats");
+    atomicAdd(reinterpret_cast<float4*>(node), make_float4(v[0], v[1], v[2], NC == 4 ? v[NC - 1] : 0.f));
+}
+
 template <int K, int NC, bool DET = false>
 __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float, K>& st, const float* u0, float m,
                             const float* A, float* __restrict__ grid, int tile_cap, unsigned char* smem,
@@ -521,10 +531,7 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
                     for (int q = 0; q < NC; ++q)
                         if (acc[q] != 0.f) atomicAdd(&tilebuf[q * vol + idx], acc[q]);
                 } else if (in_grid(kp, i, j, k)) {
-                    const long long nd = node_of(kp, i, j, k);
-#pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        if (acc[q] != 0.f) atomicAdd(&grid[nd * 4 + q], acc[q]);
+                    add_node<NC>(grid + node_of(kp, i, j, k) * 4, acc);
                 }
             }
         }
@@ -569,10 +576,7 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
             const int jj = rr % e1, ii = rr / e1;
             const int i = b0 + ii, j = b1 + jj, k = b2 + kk;
             if (!in_grid(kp, i, j, k)) continue;
-            const long long nd = node_of(kp, i, j, k);
-#pragma unroll
-            for (int q = 0; q < NC; ++q)
-                if (v[q] != 0.f) atomicAdd(&grid[nd * 4 + q], v[q]);
+            add_node<NC>(grid + node_of(kp, i, j, k) * 4, v);
         }
     }
 }
