@@ -421,6 +421,31 @@ enum {
     BR_DR_REGULARISED = 8  // rotation-derivative solve regularised (det A < 1e-6, Elasticity.cpp:57-117)
 };
 
+// The FP64 guard of the polar decomposition: R from the FP64 SVD of F.  Out
+// of line, like the guards below: these run only for F near inversion, and
+// their double temporaries would otherwise count against the registers of
+// every kernel that forms the stress or its VJP.
+template <typename R>
+static __host__ __device__ __noinline__ void polar_guard(const R* F, R* Rm)
+{
+    double Fd[9], Rd[9];
+    for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
+    polar_svd(Fd, Rd);
+    for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+}
+
+// S = sym(R^T F), the stretch of F = R S for a known rotation factor R
+template <typename R>
+MPM_HD void polar_stretch(const R* F, const R* Rm, R* S)
+{
+    R RtF[9];
+    mulTN3(Rm, F, RtF);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S[r * 3 + c] = R(0.5) * (RtF[r * 3 + c] + RtF[c * 3 + r]);
+}
+
 // F = R S.  The FP32 path uses Newton when F is safely away from inversion
 // and the FP64 SVD otherwise (the FP64 guard).
 template <typename R>
@@ -431,18 +456,15 @@ MPM_HD void polar(const R* F, R* Rm, R* S, unsigned* fl = nullptr)
     R ref = n2 * sqrt(n2) * R(0.19245008972987526);  // (|F|_F / sqrt 3)^3
     bool ok = (J > R(0.05) * ref) && polar_newton(F, Rm);
     if (!ok) {
-        double Fd[9], Rd[9];
-        for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
-        polar_svd(Fd, Rd);
-        for (int i = 0; i < 9; ++i) Rm[i] = (R)Rd[i];
+        // the guard works on copies, so the caller's arrays are never
+        // address-taken (they stay in registers on the common path)
+        R Fg[9], Rg[9];
+        for (int i = 0; i < 9; ++i) Fg[i] = F[i];
+        polar_guard(Fg, Rg);
+        for (int i = 0; i < 9; ++i) Rm[i] = Rg[i];
         if (fl) *fl |= BR_POLAR_SVD;
     }
-    R RtF[9];
-    mulTN3(Rm, F, RtF);
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) S[r * 3 + c] = R(0.5) * (RtF[r * 3 + c] + RtF[c * 3 + r]);
+    polar_stretch(F, Rm, S);
 }
 
 // --------------------------------------------------------- constitutive
@@ -457,6 +479,22 @@ struct Inv {
     R Jraw, Jc, Jm1c;
     R Fit[9];
 };
+
+// Below J = 0.25: J, the clamped J and F^{-T} in FP64 (out of line)
+template <typename R>
+static __host__ __device__ __noinline__ void invariants_guard(const R* F, Inv<R>& v, unsigned* fl)
+{
+    double Fd[9], c[9];
+    for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
+    cof3(Fd, c);
+    double Jd = Fd[0] * c[0] + Fd[1] * c[1] + Fd[2] * c[2];
+    for (int i = 0; i < 9; ++i) v.Fit[i] = (R)(c[i] / Jd);
+    double Jcd = Jd > 1e-6 ? Jd : 1e-6;
+    v.Jraw = (R)Jd;
+    v.Jc = (R)Jcd;
+    v.Jm1c = (R)(Jcd - 1.0);
+    if (fl) *fl |= BR_INV_FP64 | (Jd > 1e-6 ? 0u : (unsigned)BR_J_CLAMP);
+}
 
 template <typename R>
 MPM_HD void invariants(const R* F, Inv<R>& v, unsigned* fl = nullptr)
@@ -473,16 +511,13 @@ MPM_HD void invariants(const R* F, Inv<R>& v, unsigned* fl = nullptr)
         v.Jc = J;
         v.Jm1c = jm1;
     } else {
-        double Fd[9], c[9];
-        for (int i = 0; i < 9; ++i) Fd[i] = (double)F[i];
-        cof3(Fd, c);
-        double Jd = Fd[0] * c[0] + Fd[1] * c[1] + Fd[2] * c[2];
-        for (int i = 0; i < 9; ++i) v.Fit[i] = (R)(c[i] / Jd);
-        double Jcd = Jd > 1e-6 ? Jd : 1e-6;
-        v.Jraw = (R)Jd;
-        v.Jc = (R)Jcd;
-        v.Jm1c = (R)(Jcd - 1.0);
-        if (fl) *fl |= BR_INV_FP64 | (Jd > 1e-6 ? 0u : (unsigned)BR_J_CLAMP);
+        R Fg[9];
+        for (int i = 0; i < 9; ++i) Fg[i] = F[i];
+        Inv<R> g;
+        unsigned f = 0;
+        invariants_guard(Fg, g, &f);
+        v = g;
+        if (fl) *fl |= f;
     }
 }
 
@@ -528,6 +563,21 @@ MPM_HD void rotation_vjp(const T* Rm, const T* S, const T* G, T* dR, unsigned* f
     mul3(Rm, W, dR);
 }
 
+// rotation_vjp in FP64 from F itself (R, S by the FP64 SVD), out of line
+template <typename R>
+static __host__ __device__ __noinline__ void rotation_vjp_guard(const R* F, const R* G, R* dR, unsigned* fl)
+{
+    double Fd[9], Rd[9], Gd[9], Sd[9], dRd[9];
+    for (int i = 0; i < 9; ++i) {
+        Fd[i] = (double)F[i];
+        Gd[i] = (double)G[i];
+    }
+    polar_svd(Fd, Rd);
+    polar_stretch(Fd, Rd, Sd);
+    rotation_vjp(Rd, Sd, Gd, dRd, fl);
+    for (int i = 0; i < 9; ++i) dR[i] = (R)dRd[i];
+}
+
 // VJP of P(F) applied to G = dL/dP; returns dL/dF.  exact == false follows
 // d2_FCE_psi_dF2_mult_by_dF (Elasticity.cpp:57-117), including its use of
 // the clamped J next to the unclamped one inside d(J F^{-T})/dF.
@@ -559,17 +609,15 @@ MPM_HD void pk_vjp(int material, bool exact, const R* F, R lam, R mu, const Inv<
             // nearly cancel, which only an inverted or near-singular F
             // reaches) makes the solve ill-conditioned, beyond what FP32
             // holds -- redo R, S and the regularised solve in FP64 from F
-            double Fd[9], Rd[9], Gd[9], RtF[9], Sd[9], dRd[9];
+            R Fg[9], Gg[9], dRg[9];
             for (int i = 0; i < 9; ++i) {
-                Fd[i] = (double)F[i];
-                Gd[i] = (double)G[i];
+                Fg[i] = F[i];
+                Gg[i] = G[i];
             }
-            polar_svd(Fd, Rd);
-            mulTN3(Rd, Fd, RtF);
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) Sd[r * 3 + c] = 0.5 * (RtF[r * 3 + c] + RtF[c * 3 + r]);
-            rotation_vjp(Rd, Sd, Gd, dRd, fl);
-            for (int i = 0; i < 9; ++i) dR[i] = (R)dRd[i];
+            unsigned f = 0;
+            rotation_vjp_guard(Fg, Gg, dRg, &f);
+            for (int i = 0; i < 9; ++i) dR[i] = dRg[i];
+            if (fl) *fl |= f;
         } else {
             rotation_vjp(Rm, S, G, dR, fl);
         }
