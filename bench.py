@@ -247,7 +247,7 @@ def run_ours(args, rank, world, device):
         n, T = w.n, w.steps
         cg, keep = build_graph(dm, w, "fp32", w.checkpoint, deterministic=args.deterministic)
         n_pad = n
-    cg.set_resort(not args.no_resort)
+    apply_resort(cg, args)
     if w.extra.get("grad_E"):
         cg.enable_lame_grads(True)
     cg.set_up_comp_graph(T + 1)
@@ -350,7 +350,9 @@ def run_ours(args, rank, world, device):
                    "tuning": tuning, "cuda_graphs": True, "deterministic": bool(args.deterministic),
                    "particle_order": ("shuffled" if args.shuffle else "cell-sorted input") +
                                      (f", advanced {args.from_rollout} steps (drifted)" if args.from_rollout else "") +
-                                     ("" if args.no_resort else ", re-sorted by cell at set-up"),
+                                     ("" if args.no_resort else ", re-sorted by cell at set-up") +
+                                     (f", and every {cg.resort_every()} layers inside the rollout"
+                                      if cg.resort_every() else ""),
                    "gradients": "layer 0: x, v, F, C, control F" + (", lam, mu (dL/dE)" if w.extra.get("grad_E")
                                                                     else "")},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
@@ -499,6 +501,16 @@ def run_render(args, device):
             "clocks": clk.summary()}
 
 
+def apply_resort(cg, args):
+    """Particle re-sorts: at set-up and inside the rollout (library defaults
+    unless switched off or set)."""
+    cg.set_resort(not args.no_resort)
+    if args.no_resort:
+        cg.set_resort_every(0)
+    elif args.resort_every is not None:
+        cg.set_resort_every(args.resort_every)
+
+
 def run_e2e(torch, dm, args, w, device, keep, tuning=None):
     """Public API with pinned host buffers: x0, v0, F0 in; dL/dx_T seed in
     (computed on the host from x_T out, like run.py's gradient injection);
@@ -512,6 +524,7 @@ def run_e2e(torch, dm, args, w, device, keep, tuning=None):
     grad_E = bool(w.extra.get("grad_E"))
     if grad_E:
         cg.enable_lame_grads(True)
+    apply_resort(cg, args)
     if tuning:  # the device arm's kernel configuration
         cg.set_tuning(tuning["tile_nodes"], tuning["scatter_mode"], tuning.get("adj_tile_nodes", -1),
                       tuning.get("gather_tile_nodes", -1), tuning.get("block_threads", -1))
@@ -788,6 +801,8 @@ def main():
     ap.add_argument("--no-det", action="store_true", help="morph500k: float atomics instead of fixed point")
     ap.add_argument("--shuffle", action="store_true", help="shuffle the particle order of the workload")
     ap.add_argument("--no-resort", action="store_true", help="keep the input particle order (no cell re-sort)")
+    ap.add_argument("--resort-every", type=int, default=None,
+                    help="re-sort inside the rollout every N layers (0 never; default: the library's choice)")
     ap.add_argument("--from-rollout", type=int, default=0,
                     help="start from the state after this many forward steps (drifted particle order)")
     args = ap.parse_args()

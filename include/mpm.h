@@ -342,6 +342,23 @@ int mpm_compgraph_set_deterministic(mpm_compgraph* cg, int on);
  * turns that off. */
 int mpm_compgraph_resort(mpm_compgraph* cg);
 int mpm_compgraph_set_resort(mpm_compgraph* cg, int on);
+/* No counterpart in the reference: re-sort inside a rollout.  A forward pass
+ * re-sorts the particles by cell at every `layers`-th layer after its start
+ * (rounded up to a multiple of the checkpoint interval: segment starts), so
+ * the particles stay in cell order as they move; each segment keeps its own
+ * order and the backward pass carries the gradients across the boundaries.
+ * Gets and sets still see the caller's order.  -1 (the default): the
+ * checkpoint interval, or 20 with the full tape, for graphs of at least 2^18
+ * particles, else never; 0: never.  Results equal those without re-sorting
+ * up to the order of float additions (bit for bit with deterministic
+ * scatters).  Gradients of layers other than the last and the control layer
+ * are the backward pass's output: a forward pass leaves them undefined. */
+int mpm_compgraph_set_resort_every(mpm_compgraph* cg, int layers);
+/* the interval in effect (0: never) */
+int mpm_compgraph_get_resort_every(const mpm_compgraph* cg, int* layers);
+/* The particle order of a layer: slot p holds the caller's particle out[p]
+ * (n ints).  Diagnostics; no counterpart in the reference. */
+int mpm_compgraph_particle_order(mpm_compgraph* cg, int layer, int* out);
 /* accumulate dL/dlambda and dL/dmu per particle over the next backward
  * passes; read them from the control layer's MPM_FIELD_GRAD_LAM/GRAD_MU */
 int mpm_compgraph_enable_lame_grads(mpm_compgraph* cg, int on);

@@ -517,6 +517,14 @@ struct Layer {
     std::shared_ptr<PCData> pc;  // null for non-stored layers of a checkpointed graph
     Buf grid;                    // grid of the step leaving this layer (lazy)
     Buf trust;                   // trust-region scale of that step (exact adjoint)
+    // In-rollout re-sort: a segment start whose particles the forward pass
+    // re-sorted by cell.  The layers of its segment share its permutation
+    // (rs_perm) and constants (rs_co, the constant planes in this order);
+    // rs_back[q] is the slot in this order of slot q of the previous
+    // segment's order, which the backward pass uses to carry the boundary
+    // gradients across.
+    bool rs_on = false;
+    Buf rs_perm, rs_back, rs_co;
 };
 
 struct Graph {
@@ -580,6 +588,12 @@ struct Graph {
     long long total_nodes = 0;
     std::vector<double> loss_hist;  // losses evaluated by the last run_optimization / optimize_single
     bool resort_on = true;           // re-sort the particles by cell at set-up
+    // re-sort inside a rollout every this many layers (at segment starts):
+    // -1 automatic (the checkpoint interval, or 20 with the full tape, for
+    // graphs of at least 2^18 particles), 0 never
+    int resort_every = -1;
+    Buf rs_work, rs_order, rs_tmp;   // sort scratch, the sort's order, plane scratch
+    std::shared_ptr<PCData> rs;      // a boundary layer's state before its re-sort
     // render gradients (stored on the host like CompGraph.h:73-76)
     std::vector<float> rgF, rgx;
     bool has_rg = false;
@@ -630,6 +644,22 @@ struct Graph {
             c.fix_reach = 6.0 * max_dx;
         }
         return c;
+    }
+
+    int resort_interval() const
+    {
+        const int k = std::max(1, opt.checkpoint_every);
+        int r = resort_every;
+        if (r < 0) r = (n() >= (1 << 18)) ? (k > 1 ? k : 20) : 0;
+        if (r > 0 && k > 1) r = ((r + k - 1) / k) * k;  // segment starts only
+        return r;
+    }
+
+    // layer i is re-sorted by a forward pass that starts at layer `start`
+    bool resort_at(int i, int start) const
+    {
+        const int r = resort_interval();
+        return r > 0 && i > start && i % r == 0 && i < (int)layers.size() - 1;
     }
 
     bool stored(int i) const
@@ -718,9 +748,12 @@ long long g_fwd_steps = 0, g_bwd_steps = 0;  // particle-layer steps executed (h
 unsigned long long g_state_epoch = 0;
 
 // Re-sort the graph's particles by (instance, cell) of layer 0's positions:
-// every particle plane of every layer (state, constants, control, gradients,
-// Adam moments, trust scales) moves to the new order in place, and the
-// layers get the composed permutation.  Grids do not depend on the order.
+// every particle plane of every layer in layer 0's order (state, constants,
+// control, gradients, Adam moments, trust scales) moves to the new order in
+// place, and those layers get the composed permutation.  Layers that an
+// in-rollout re-sort put in an order of their own keep it; the first of them
+// has its map back re-based on the new order.  Grids do not depend on the
+// order.
 template <typename R>
 void graph_resort(Graph& G)
 {
@@ -746,8 +779,17 @@ void graph_resort(Graph& G)
         todo.push_back({b.get(), es});
         big = std::max(big, b->bytes);
     };
-    for (Layer& L : G.layers) {
-        if (!L.pc) continue;
+    const Buf own = d0.perm;  // layers in layer 0's order share this (or none)
+    auto same = [&](const PCData* d) { return d && d->perm == own; };
+    int first_rs = -1;
+    for (size_t i = 1; i < G.layers.size(); ++i)
+        if (G.layers[i].rs_on) {
+            first_rs = (int)i;
+            break;
+        }
+    for (size_t i = 0; i < G.layers.size(); ++i) {
+        Layer& L = G.layers[i];
+        if (!L.pc || (first_rs >= 0 && (int)i >= first_rs)) continue;
         PCData& d = *L.pc;
         if (d.have_state) add(d.st, (int)sizeof(R));
         add(d.co, (int)sizeof(R));
@@ -772,15 +814,21 @@ void graph_resort(Graph& G)
     Buf perm = make_buf(sizeof(int) * n, s, false);
     if (d0.perm) launch_gather_planes<float>(n, 1, n, order.as<int>(), d0.perm->as<float>(), perm->as<float>(), s);
     else ck(cudaMemcpyAsync(perm->p, order.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s), "copy");
+    // the first re-sorted boundary maps its order back to the new one
+    if (first_rs >= 0) {
+        Buf& back = G.layers[first_rs].rs_back;
+        launch_gather_planes<float>(n, 1, n, order.as<int>(), back->as<float>(), tmp.as<float>(), s);
+        ck(cudaMemcpyAsync(back->p, tmp.p, sizeof(int) * n, cudaMemcpyDeviceToDevice, s), "copy");
+    }
     check_launch("resort");
     ck(cudaStreamSynchronize(s), "sync");
-    for (Layer& L : G.layers)
-        if (L.pc) L.pc->perm = perm;
-    G.base->perm = perm;
+    for (size_t i = 0; i < G.layers.size(); ++i)
+        if (same(G.layers[i].pc.get()) && !(first_rs >= 0 && (int)i >= first_rs)) G.layers[i].pc->perm = perm;
+    if (same(G.base.get())) G.base->perm = perm;
     for (auto* q : {&G.ping, &G.pong})
-        if (*q) (*q)->perm = perm;
+        if (same(q->get())) (*q)->perm = perm;
     for (auto& q : G.seg)
-        if (q) q->perm = perm;
+        if (same(q.get())) q->perm = perm;
 }
 
 // One forward step: layer i -> layer i+1 (ForwardSimulation.cpp:159-185)
@@ -968,6 +1016,8 @@ struct Sig {
             return;
         }
         add(d->st);
+        add(d->co);
+        add(d->perm);
         add(d->grads);
         add(d->gctl);
         add(d->dfc_zero ? nullptr : d->dfc->p);
@@ -1047,6 +1097,98 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
     replay();
 }
 
+// Buffers of the in-rollout re-sort of boundary layer b (allocated before a
+// pass is recorded, so the recorded pass allocates nothing)
+void prepare_resort(Graph& G, int b, cudaStream_t s)
+{
+    PCData& d = *G.layers[b].pc;
+    const size_t n = (size_t)d.n;
+    const size_t temp = SortWork::temp_for(d.n);
+    ensure(G.rs_work, 2 * 8 * n + 4 * n + temp + 256, s, false);
+    ensure(G.rs_order, 4 * n, s, false);
+    Layer& L = G.layers[b];
+    ensure(L.rs_perm, 4 * n, s, false);
+    ensure(L.rs_back, 4 * n, s, false);
+    ensure(L.rs_co, d.planes_bytes(CO_N), s, false);
+    // the largest per-layer plane set moved in place: 27 planes of double
+    ensure(G.rs_tmp, (size_t)27 * d.ld * 8, s, false);
+    if (!G.rs || G.rs->n != d.n) G.rs = shell_like(d, s, true);
+    if (!d.st) d.st = make_buf(d.planes_bytes(ST_N), s, false);
+}
+
+SortWork sort_work(const Graph& G)
+{
+    SortWork w;
+    const size_t n = (size_t)G.n();
+    char* p = G.rs_work->as<char>();
+    w.keys_in = reinterpret_cast<unsigned long long*>(p);
+    w.keys_out = reinterpret_cast<unsigned long long*>(p + 8 * n);
+    w.vals = reinterpret_cast<int*>(p + 16 * n);
+    const size_t off = (20 * n + 255) & ~(size_t)255;
+    w.temp = p + off;
+    w.temp_bytes = G.rs_work->bytes - off;
+    return w;
+}
+
+// In-place permutation of k planes (element size es) through the order of
+// the current re-sort, via the plane scratch
+template <typename R>
+void permute_planes(Graph& G, const Buf& b, int k, int es, const int* order, cudaStream_t s)
+{
+    if (!b) return;
+    const int n = G.n();
+    const long long ld = G.ld();
+    if (es == 8) launch_gather_planes<double>(n, k, ld, order, b->as<double>(), G.rs_tmp->as<double>(), s);
+    else launch_gather_planes<float>(n, k, ld, order, b->as<float>(), G.rs_tmp->as<float>(), s);
+    ck(cudaMemcpyAsync(b->p, G.rs_tmp->p, (size_t)k * ld * es, cudaMemcpyDeviceToDevice, s), "copy");
+}
+
+// Re-sort of boundary layer b inside a forward pass: G.rs holds layer b's
+// state in the previous segment's order (permutation prev_perm, constants
+// prev_co).  Sorts by cell, writes the state in the new order into layer b,
+// and forms the new permutation, the map back and the constants in the new
+// order.  The Adam moments of the segment's layers and the gradients of the
+// graph's last layer (set between passes) move with the particles, from the
+// order each layer held before this pass (old_perm) to the new one; other
+// gradients are the backward pass's output and are rewritten by it.
+template <typename R>
+void resort_boundary(Graph& G, const StepCfg& c, int b, int seg_end, const Buf& prev_perm, const Buf& prev_co,
+                     const std::vector<Buf>& old_perm, cudaStream_t s)
+{
+    PCData& d = *G.layers[b].pc;
+    Layer& L = G.layers[b];
+    const int n = d.n;
+    const long long ld = d.ld;
+    int* order = G.rs_order->as<int>();
+    const SortWork w = sort_work(G);
+    cell_order_async<R>(c, G.inst.empty() ? nullptr : G.inst.data(), (int)G.inst.size(), n, ld,
+                        G.rs->st->as<R>() + ST_X * ld, order, w, s);
+    check_launch("resort keys/sort");
+    // after the sort its key buffers are free: the new permutation goes to
+    // scratch first, so that the old orders (one may be this layer's own
+    // permutation buffer) are still readable below
+    int* pnew = reinterpret_cast<int*>(w.keys_in);
+    int* inv = pnew + n;
+    int* rel = reinterpret_cast<int*>(w.keys_out);
+    launch_perm_compose(n, order, prev_perm ? prev_perm->as<int>() : nullptr, pnew, L.rs_back->as<int>(), s);
+    launch_gather_planes<R>(n, ST_N, ld, order, G.rs->st->as<R>(), d.st->as<R>(), s);
+    launch_gather_planes<R>(n, CO_N, ld, order, prev_co->as<R>(), L.rs_co->as<R>(), s);
+    // planes kept across passes (Adam moments; the last layer's gradients,
+    // set between passes) move from the order their layer held before this
+    // pass to the new one
+    const int last = (int)G.layers.size() - 1;
+    for (int i = b; i < seg_end; ++i) {
+        PCData* q = G.layers[i].pc.get();
+        if (!q || !(q->adam || (i == last && q->grads))) continue;
+        const Buf& op = old_perm[i];
+        launch_perm_relative(n, op ? op->as<int>() : nullptr, pnew, inv, rel, s);
+        if (q->adam) permute_planes<R>(G, q->adam, 27, 8, rel, s);
+        if (i == last && q->grads) permute_planes<R>(G, q->grads, ST_N, (int)sizeof(R), rel, s);
+    }
+    ck(cudaMemcpyAsync(L.rs_perm->p, pnew, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s), "copy");
+    check_launch("resort");
+}
+
 // ComputeForwardPass (CompGraph.cpp:131-141).  With checkpointing the
 // non-stored layers pass through two scratch states and one scratch grid.
 template <typename R>
@@ -1061,6 +1203,66 @@ void graph_forward(Graph& G, int start)
     if (!G.layers[start].pc || !G.layers[start].pc->have_state)
         fail(MPM_ERR_STATE, "layer %d is not stored; forward passes of a checkpointed graph start at a stored layer",
              start);
+    // in-rollout re-sort points, and the order (permutation, constants) of
+    // each layer of the pass: the start layer's, or its segment start's
+    std::vector<int> bounds;
+    for (int i = start + 1; i < L - 1; ++i)
+        if (G.resort_at(i, start)) bounds.push_back(i);
+    for (int b : bounds) prepare_resort(G, b, s);
+    std::vector<Buf> old_perm(L);  // each layer's order before this pass
+    for (int i = 0; i < L; ++i)
+        if (G.layers[i].pc) old_perm[i] = G.layers[i].pc->perm;
+    {
+        Buf perm = G.layers[start].pc->perm, co = G.layers[start].pc->co;
+        size_t bi = 0;
+        for (int i = start + 1; i < L; ++i) {
+            Layer& la = G.layers[i];
+            la.rs_on = bi < bounds.size() && bounds[bi] == i;
+            if (la.rs_on) {
+                perm = la.rs_perm;
+                co = la.rs_co;
+                ++bi;
+            }
+            if (la.pc) {
+                la.pc->perm = perm;
+                la.pc->co = co;
+            }
+        }
+    }
+    // layers that change order without a re-sort in this pass (the re-sort
+    // interval changed since the last one): their kept planes move now
+    {
+        std::vector<int> seg_of(L, -1);
+        for (size_t j = 0; j < bounds.size(); ++j)
+            for (int i = bounds[j]; i < (j + 1 < bounds.size() ? bounds[j + 1] : L); ++i) seg_of[i] = (int)j;
+        for (int i = start + 1; i < L; ++i) {
+            PCData* q = G.layers[i].pc.get();
+            if (!q || seg_of[i] >= 0 || old_perm[i] == q->perm) continue;
+            if (!(q->adam || (i == L - 1 && q->grads))) continue;
+            const int n = q->n;
+            DevBuf inv(sizeof(int) * n), rel(sizeof(int) * n), ident(sizeof(int) * n);
+            const int* pn = q->perm ? q->perm->as<int>() : nullptr;
+            if (!pn) {
+                std::vector<int> h(n);
+                for (int t = 0; t < n; ++t) h[t] = t;
+                ck(cudaMemcpyAsync(ident.p, h.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s), "H2D");
+                ck(cudaStreamSynchronize(s), "sync");
+                pn = ident.as<int>();
+            }
+            launch_perm_relative(n, old_perm[i] ? old_perm[i]->as<int>() : nullptr, pn, inv.as<int>(),
+                                 rel.as<int>(), s);
+            auto move = [&](const Buf& b, int k, int es) {
+                DevBuf tmp((size_t)k * q->ld * es);
+                if (es == 8) launch_gather_planes<double>(n, k, q->ld, rel.as<int>(), b->as<double>(), tmp.as<double>(), s);
+                else launch_gather_planes<float>(n, k, q->ld, rel.as<int>(), b->as<float>(), tmp.as<float>(), s);
+                ck(cudaMemcpyAsync(b->p, tmp.p, tmp.bytes, cudaMemcpyDeviceToDevice, s), "copy");
+                ck(cudaStreamSynchronize(s), "sync");
+            };
+            if (q->adam) move(q->adam, 27, 8);
+            if (i == L - 1 && q->grads) move(q->grads, ST_N, (int)sizeof(R));
+            check_launch("reorder");
+        }
+    }
     Sig sig;
     sig.add_cfg(c);
     sig.add((unsigned long long)L);
@@ -1068,6 +1270,18 @@ void graph_forward(Graph& G, int start)
         sig.add_pc(G.layers[i].pc.get());
         sig.add(G.layers[i].grid);
         sig.add(G.layers[i].trust);
+    }
+    for (int b : bounds) {
+        sig.add((unsigned long long)b);
+        sig.add(G.layers[b].rs_perm);
+        sig.add(G.layers[b].rs_back);
+        sig.add(G.layers[b].rs_co);
+    }
+    if (!bounds.empty()) {
+        sig.add_pc(G.rs.get());
+        sig.add(G.rs_work);
+        sig.add(G.rs_order);
+        sig.add(G.rs_tmp);
     }
     sig.add_pc(G.ping.get());
     sig.add_pc(G.pong.get());
@@ -1095,26 +1309,50 @@ void graph_forward(Graph& G, int start)
         PCData* cur = G.layers[start].pc.get();
         begin_fix_pass(G, c, *cur, s);
         std::vector<StepBufs> plan;
+        Buf prev_perm = cur->perm, prev_co = cur->co;
+        size_t bi = 0;
         for (int i = start; i < L - 1; ++i) {
             PCData* nxt;
             const bool in_tail = keep_tail && i >= tail_lo;
-            if (G.stored(i + 1)) {
+            const bool boundary = bi < bounds.size() && bounds[bi] == i + 1;
+            if (boundary) {
+                nxt = G.rs.get();  // re-sorted into layer i+1 below
+            } else if (G.stored(i + 1)) {
                 nxt = G.layers[i + 1].pc.get();
                 if (!nxt->st) nxt->st = make_buf(cur->planes_bytes(ST_N), s, false);
             } else if (in_tail) {
                 auto& q = G.seg[i + 1 - tail_lo];
                 const PCData& lo_pc = *G.layers[tail_lo].pc;
                 if (!q || q->n != lo_pc.n) q = shell_like(lo_pc, s, true);
+                q->co = lo_pc.co;
+                q->perm = lo_pc.perm;
                 nxt = q.get();
             } else {
                 auto& tmp = (cur == G.ping.get()) ? G.pong : G.ping;
                 if (!tmp || tmp->n != cur->n) tmp = shell_like(*cur, s, true);
+                tmp->co = cur->co;
+                tmp->perm = cur->perm;
                 nxt = tmp.get();
             }
             if (full) plan.push_back({cur, nxt, &G.layers[i].grid, &G.layers[i].trust});
             else if (in_tail) plan.push_back({cur, nxt, &G.sgrid[i - tail_lo], &G.strust[i - tail_lo]});
             else plan.push_back({cur, nxt, ((i - start) & 1) ? &G.fgrid2 : &G.fgrid, &G.ftrust});
             cur = nxt;
+            if (boundary) {
+                // the steps so far, then the new segment's order
+                run_forward_steps<R>(c, plan, s);
+                plan.clear();
+                const int b = i + 1;
+                const int seg_end = bi + 1 < bounds.size() ? bounds[bi + 1] : L;
+                resort_boundary<R>(G, c, b, seg_end, prev_perm, prev_co, old_perm, s);
+                // as for any layer a step writes: state present, control zero
+                G.layers[b].pc->dfc_zero = true;
+                G.layers[b].pc->have_state = true;
+                prev_perm = G.layers[b].rs_perm;
+                prev_co = G.layers[b].rs_co;
+                cur = G.layers[b].pc.get();
+                ++bi;
+            }
         }
         run_forward_steps<R>(c, plan, s);
     });
@@ -1160,6 +1398,30 @@ void inject_render_grads(Graph& G)
     say("[C++] Render gradients injected (L_tot = L_phys + L_render)\n");
 }
 
+// A backward pass crossing re-sorted boundary b (layer b in its own order,
+// layer b-1 in the previous segment's): the gradients of layer b, and its
+// state when with_state, in the previous order in G.ping, and the running
+// Lame gradient sums carried to that order.  Without with_state G.ping
+// already holds layer b's state in the previous order (the segment's
+// recompute leaves it there).
+template <typename R>
+PCData* back_boundary(Graph& G, int b, bool with_state, cudaStream_t s)
+{
+    Layer& L = G.layers[b];
+    PCData& d = *L.pc;
+    PCData& o = *G.ping;
+    const int n = d.n;
+    const long long ld = d.ld;
+    const int* back = L.rs_back->as<int>();
+    if (with_state) launch_gather_planes<R>(n, ST_N, ld, back, d.st->as<R>(), o.st->as<R>(), s);
+    ensure_grads(d, s);
+    ensure_grads(o, s);
+    launch_gather_planes<R>(n, ST_N, ld, back, d.grads->as<R>(), o.grads->as<R>(), s);
+    if (G.lame_on && G.glame) permute_planes<R>(G, G.glame, 2, (int)sizeof(R), back, s);
+    check_launch("boundary");
+    return &o;
+}
+
 template <typename R>
 void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cudaStream_t s, bool tail_ok);
 
@@ -1191,6 +1453,17 @@ void graph_backward(Graph& G, int control)
         sig.add(G.layers[i].grid);
         sig.add(G.layers[i].trust);
     }
+    bool crosses = false;
+    for (int i = control + 1; i < L; ++i)
+        if (G.layers[i].rs_on) {
+            crosses = true;
+            sig.add((unsigned long long)i);
+            sig.add(G.layers[i].rs_back);
+        }
+    if (crosses) {
+        if (!G.ping || G.ping->n != G.n()) G.ping = shell_like(*G.layers[control].pc, s, true);
+        sig.add(G.rs_tmp);
+    }
     sig.add(G.adj);
     sig.add((unsigned long long)G.lame_on);
     sig.add(G.glame);
@@ -1212,7 +1485,9 @@ void graph_backward(Graph& G, int control)
         if (k == 1) {
             for (int i = L - 2; i >= control; --i) {
                 Layer& la = G.layers[i];
-                step_backward<R>(G, c, *la.pc, *G.layers[i + 1].pc, la.grid, la.trust, s);
+                PCData* nb = G.layers[i + 1].pc.get();
+                if (G.layers[i + 1].rs_on) nb = back_boundary<R>(G, i + 1, true, s);
+                step_backward<R>(G, c, *la.pc, *nb, la.grid, la.trust, s);
             }
             return;
         }
@@ -1239,9 +1514,13 @@ void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cu
         S[cnt - 1] = G.layers[hi].pc.get();
         for (int j = 1; j < cnt - 1; ++j) {
             if (!G.seg[j] || G.seg[j]->n != S[0]->n) G.seg[j] = shell_like(*S[0], s, true);
+            G.seg[j]->co = S[0]->co;  // the segment's order (re-sorts give each its own)
+            G.seg[j]->perm = S[0]->perm;
             S[j] = G.seg[j].get();
         }
         if (!G.ping || G.ping->n != S[0]->n) G.ping = shell_like(*S[0], s, true);
+        G.ping->co = S[0]->co;
+        G.ping->perm = S[0]->perm;
         // the last segment, as the forward pass left it, needs no recompute
         if (!(tail_ok && hi == L - 1)) {
             std::vector<StepBufs> plan;
@@ -1253,6 +1532,9 @@ void backward_segments(Graph& G, const StepCfg& c, int control, int L, int k, cu
             }
             run_forward_steps<R>(c, plan, s);
         }
+        // a re-sorted boundary: layer hi in this segment's order (the
+        // recompute's last state is in G.ping), with its gradients carried over
+        if (G.layers[hi].rs_on && hi < L - 1) S[cnt - 1] = back_boundary<R>(G, hi, false, s);
         const int stop = std::max(control, lo);
         for (int i = hi - 1; i >= stop; --i) {
             const int j = i - lo;
@@ -1378,6 +1660,7 @@ void graph_set_up(Graph& G, int num_layers)
         }
         G.layers[i].grid.reset();
         G.layers[i].trust.reset();
+        G.layers[i].rs_on = false;
     }
 }
 
@@ -2327,6 +2610,7 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
         T.total_nodes = G.total_nodes;
         T.stream = s;
         T.resort_on = false;  // shares G's constant planes: never permute them from here
+        T.resort_every = 0;
         T.base = clone_pc(*G.layers[layer].pc, s, true);
         T.base->grads.reset();
         T.layers.resize(1);
@@ -2443,6 +2727,42 @@ int mpm_compgraph_set_resort(mpm_compgraph* cg, int on)
     return guard([&] {
         check_cg(cg);
         cg->g.resort_on = on != 0;
+    });
+}
+
+int mpm_compgraph_set_resort_every(mpm_compgraph* cg, int layers)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (layers < -1) fail(MPM_ERR_ARG, "resort interval must be -1 (automatic), 0 (never) or positive");
+        cg->g.resort_every = layers;
+    });
+}
+
+int mpm_compgraph_get_resort_every(const mpm_compgraph* cg, int* layers)
+{
+    return guard([&] {
+        check_cg(cg);
+        if (!layers) fail(MPM_ERR_ARG, "null output");
+        *layers = cg->g.resort_interval();
+    });
+}
+
+int mpm_compgraph_particle_order(mpm_compgraph* cg, int layer, int* out)
+{
+    return guard([&] {
+        check_cg(cg);
+        Graph& G = cg->g;
+        if (layer < 0 || layer >= (int)G.layers.size())
+            fail(MPM_ERR_RANGE, "layer %d out of range [0, %d)", layer, (int)G.layers.size());
+        if (!out) fail(MPM_ERR_ARG, "null output");
+        const PCData& d = *G.layers[layer].pc;
+        ck(cudaStreamSynchronize(G.stream), "sync");
+        if (d.perm) {
+            ck(cudaMemcpy(out, d.perm->p, sizeof(int) * d.n, cudaMemcpyDeviceToHost), "D2H");
+        } else {
+            for (int i = 0; i < d.n; ++i) out[i] = i;
+        }
     });
 }
 

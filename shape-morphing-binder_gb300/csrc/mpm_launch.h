@@ -158,6 +158,27 @@ void launch_gather_planes(int n, int k, long long ld, const int* order, const R*
 template <typename R>
 bool cell_order(const StepCfg& c, const InstHost* inst, int ninst, int n, long long ld, const R* x, int* order,
                 cudaStream_t s);
+// Scratch of an in-rollout re-sort (cell_order_async), allocated once per
+// graph: keys, values and CUB's temporary storage for n slots
+struct SortWork {
+    unsigned long long* keys_in = nullptr;
+    unsigned long long* keys_out = nullptr;
+    int* vals = nullptr;
+    void* temp = nullptr;
+    size_t temp_bytes = 0;
+    static size_t temp_for(int n);
+};
+// cell_order without allocations or synchronisation (stream-ordered, safe
+// under stream capture)
+template <typename R>
+void cell_order_async(const StepCfg& c, const InstHost* inst, int ninst, int n, long long ld, const R* x,
+                      int* order, const SortWork& w, cudaStream_t s);
+// perm_new[i] = perm_old[order[i]] (perm_old null: order[i]); back[order[i]] = i
+void launch_perm_compose(int n, const int* order, const int* perm_old, int* perm_new, int* back, cudaStream_t s);
+// rel[i] = slot under perm_old of the particle perm_new puts at slot i
+// (perm_old null: the identity); inv_scratch: n ints
+void launch_perm_relative(int n, const int* perm_old, const int* perm_new, int* inv_scratch, int* rel,
+                          cudaStream_t s);
 template <typename R>
 void launch_axpy_planes(int n, int k, long long ld, R alpha, const R* x, R* y, cudaStream_t s);
 template <typename R>

@@ -380,6 +380,24 @@ class CompGraph:
         """Re-sort at set_up_comp_graph (default on)."""
         check(lib.mpm_compgraph_set_resort(self._h, int(bool(on))))
 
+    def set_resort_every(self, layers=-1):
+        """Re-sort inside a rollout every `layers` layers (segment starts);
+        -1 automatic, 0 never (additive)."""
+        check(lib.mpm_compgraph_set_resort_every(self._h, int(layers)))
+
+    def resort_every(self) -> int:
+        """The in-rollout re-sort interval in effect (0: never)."""
+        v = C.c_int()
+        check(lib.mpm_compgraph_get_resort_every(self._h, C.byref(v)))
+        return v.value
+
+    def particle_order(self, layer: int) -> np.ndarray:
+        """Slot p of the layer's device planes holds the caller's particle
+        out[p] (diagnostics)."""
+        out = np.empty(len(self.get_point_cloud(layer)), np.int32)
+        check(lib.mpm_compgraph_particle_order(self._h, int(layer), out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
     def set_deterministic(self, on=True):
         """Fixed-point node sums (FP32 graphs): bitwise reproducible passes."""
         check(lib.mpm_compgraph_set_deterministic(self._h, int(bool(on))))

@@ -113,6 +113,9 @@ _SIGS = {
     "gs_render": [_vp, _vp, C.c_int, _vp, _vp, C.c_size_t, _vp, _vp],
     "gs_backward": [_vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "mpm_compgraph_set_resort": [_vp, C.c_int],
+    "mpm_compgraph_set_resort_every": [_vp, C.c_int],
+    "mpm_compgraph_get_resort_every": [_vp, _ip],
+    "mpm_compgraph_particle_order": [_vp, C.c_int, _ip],
     "mpm_compgraph_loss_history": [_vp, _dp, C.c_int, _ip],
     "mpm_step_count": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
     "mpm_compgraph_get_tuning": [_vp, _ip, _ip],

@@ -34,7 +34,8 @@ def golden_params(gd, exact=False):
 
 
 def make_graph(dm, s, grid, prm, precision="fp32", adjoint="reference", layers=2, checkpoint_every=1,
-               kernel="cubic", material="fcr", target_mass=None, deterministic=False, resort=True):
+               kernel="cubic", material="fcr", target_mass=None, deterministic=False, resort=True,
+               resort_every=None):
     """CompGraph on the GPU holding state s in layer 0 (oracle.State)."""
     dtype = np.float64 if precision == "fp64" else np.float32
     pc = dm.PointCloud.from_arrays(s.x.astype(dtype), v=s.v.astype(dtype), F=s.F.astype(dtype),
@@ -50,6 +51,8 @@ def make_graph(dm, s, grid, prm, precision="fp32", adjoint="reference", layers=2
     cg.set_sim_params(dt=prm.dt, drag=prm.drag, smoothing=prm.smoothing, f_ext=prm.f_ext,
                       bulk_viscosity=prm.bulk_visc, j_min=prm.j_min)
     cg.set_resort(resort)
+    if resort_every is not None:
+        cg.set_resort_every(resort_every)
     cg.set_up_comp_graph(layers)
     return cg, (pc, g, tg)
 
