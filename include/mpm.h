@@ -348,7 +348,7 @@ int mpm_compgraph_set_resort(mpm_compgraph* cg, int on);
  * the particles stay in cell order as they move; each segment keeps its own
  * order and the backward pass carries the gradients across the boundaries.
  * Gets and sets still see the caller's order.  -1 (the default): the
- * checkpoint interval, or 20 with the full tape, for graphs of at least 2^18
+ * checkpoint interval, or 20 with the full tape, for graphs of at least 2^16
  * particles, else never; 0: never.  Results equal those without re-sorting
  * up to the order of float additions (bit for bit with deterministic
  * scatters).  Gradients of layers other than the last and the control layer

@@ -590,7 +590,7 @@ struct Graph {
     bool resort_on = true;           // re-sort the particles by cell at set-up
     // re-sort inside a rollout every this many layers (at segment starts):
     // -1 automatic (the checkpoint interval, or 20 with the full tape, for
-    // graphs of at least 2^18 particles), 0 never
+    // graphs of at least 2^16 particles), 0 never
     int resort_every = -1;
     Buf rs_work, rs_order, rs_tmp;   // sort scratch, the sort's order, plane scratch
     std::shared_ptr<PCData> rs;      // a boundary layer's state before its re-sort
@@ -650,7 +650,7 @@ struct Graph {
     {
         const int k = std::max(1, opt.checkpoint_every);
         int r = resort_every;
-        if (r < 0) r = (n() >= (1 << 18)) ? (k > 1 ? k : 20) : 0;
+        if (r < 0) r = (n() >= (1 << 16)) ? (k > 1 ? k : 20) : 0;
         if (r > 0 && k > 1) r = ((r + k - 1) / k) * k;  // segment starts only
         return r;
     }

@@ -135,3 +135,19 @@ def test_resort_in_rollout_optimiser_steps(dm):
         for la, lb in zip(r[:-1], b[:-1]):
             assert abs(la - lb) <= 1e-4 * abs(lb)
         assert norm_err(r[-1], b[-1]) < 1e-4
+
+
+@pytest.mark.parametrize("checkpoint_every", [1, 3])
+def test_resort_in_rollout_fp64_matches_oracle(dm, orc, checkpoint_every):
+    """FP64: the re-sort changes only the order of additions, so the rollout
+    and its gradients match the oracle to double-precision noise."""
+    s0, g, rng = _spinning(4)
+    prm = O.Params(dt=1e-3, drag=0.1, smoothing=0.1, exact=True)
+    T = 9
+    seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
+    a, cg, _ = _run(dm, s0, g, prm, T, seed_gx, 3, checkpoint_every=checkpoint_every, precision="fp64")
+    assert not np.array_equal(cg.particle_order(3), cg.particle_order(0))
+    xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
+    assert rel_err(a["xT"], xw) < 1e-10
+    assert norm_err(a["gv"], gw.v) < 1e-9
+    assert norm_err(a["gdFc"], gw.Ft) < 1e-9
