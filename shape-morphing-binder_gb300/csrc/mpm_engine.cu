@@ -2616,7 +2616,7 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
         T.layers.resize(1);
         T.layers[0].pc = T.base;
         const int tiles[] = {0, 512, 1024, 2048};
-        const int adj_tiles[] = {512, 1024, 2048};
+        const int adj_tiles[] = {0, 512, 1024, 2048};
         const int gather_tiles[] = {1024, 2048, 2816};
         double best = 1e300;
         int bt = -1, bm = -1, ba = -1, bg = -1, bth = 256;
@@ -2675,7 +2675,7 @@ int mpm_compgraph_autotune_from(mpm_compgraph* cg, int layer, int steps, int* be
                     field = pick;
                     return pick;
                 };
-                ba = sweep(adj_tiles, 3, T.adj_tile_nodes, 1024);
+                ba = sweep(adj_tiles, 4, T.adj_tile_nodes, 1024);
                 bg = sweep(gather_tiles, 3, T.gather_tile_nodes, 2048);
             }
             // 4. threads (= particles) per block of the step kernels
