@@ -394,9 +394,15 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
     unsigned long long* tilefix = reinterpret_cast<unsigned long long*>(tilebuf);
     bool ovf = false;
     __shared__ int box[6];
+    // Without a node tile (tile_cap 0, uniform over the launch) a warp reads
+    // only its own lanes' records: no block-wide bounding box and no block
+    // barriers, only the warp's own.
+    const bool blockwide = tile_cap > 0;
     // 1. this lane's record, the block's bounding box of stencil bases
-    if (t < 3) box[t] = INT_MAX;
-    else if (t < 6) box[t] = INT_MIN;
+    if (blockwide) {
+        if (t < 3) box[t] = INT_MAX;
+        else if (t < 6) box[t] = INT_MIN;
+    }
     if (valid) {
         float* r = recs + (size_t)t * kRec;
         r[0] = u0[0];
@@ -413,15 +419,19 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
                 r[17 + 2 * (a * K + o)] = st.g[a][o];
             }
     }
-    __syncthreads();
+    if (blockwide) {
+        __syncthreads();
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int lo = __reduce_min_sync(0xffffffffu, valid ? st.base[a] : INT_MAX);
-        const int hi = __reduce_max_sync(0xffffffffu, valid ? st.base[a] : INT_MIN);
-        if (lane == 0) {
-            atomicMin(&box[a], lo);
-            atomicMax(&box[3 + a], hi);
+        for (int a = 0; a < 3; ++a) {
+            const int lo = __reduce_min_sync(0xffffffffu, valid ? st.base[a] : INT_MAX);
+            const int hi = __reduce_max_sync(0xffffffffu, valid ? st.base[a] : INT_MIN);
+            if (lane == 0) {
+                atomicMin(&box[a], lo);
+                atomicMax(&box[3 + a], hi);
+            }
         }
+    } else {
+        __syncwarp();
     }
     // 2. groups of lanes sharing a stencil base (not necessarily contiguous:
     //    particles drift across cells between sorts)
@@ -431,11 +441,11 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
               : ~0ull;
     const unsigned grp = __match_any_sync(0xffffffffu, key);
     unsigned todo = __ballot_sync(0xffffffffu, valid);
-    __syncthreads();
+    if (blockwide) __syncthreads();
     // 3. node tile over the bounding box, if it fits
     bool tile = false;
     int b0 = 0, b1 = 0, b2 = 0, e1 = 0, e2 = 0, vol = 0;
-    if (tile_cap > 0 && box[0] != INT_MAX) {
+    if (blockwide && box[0] != INT_MAX) {
         const long long x0 = (long long)box[3] - box[0] + K, x1 = (long long)box[4] - box[1] + K,
                         x2 = (long long)box[5] - box[2] + K;
         if (x0 > 0 && x1 > 0 && x2 > 0 && x0 <= tile_cap && x1 <= tile_cap && x2 <= tile_cap &&
@@ -454,7 +464,7 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
             }
         }
     }
-    __syncthreads();
+    if (blockwide) __syncthreads();
     // 4. each warp walks its runs; lane owns stencil nodes lane and lane+32
     constexpr int NODES = K * K * K;
     const int n0 = lane, n1 = lane + 32;
@@ -536,7 +546,7 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
             }
         }
     }
-    __syncthreads();
+    if (blockwide) __syncthreads();
     // 5. flush the tile
     if constexpr (DET) {
         if (__any_sync(0xffffffffu, ovf) && lane == 0) atomicOr(&fx->ctl[3], 1u);

@@ -356,7 +356,7 @@ def test_autotune_picks_a_valid_configuration(dm, orc):
     cg, keep = make_graph(dm, s0, g, prm, precision="fp32", layers=3)
     res = cg.autotune(steps=2)
     assert res["tile_nodes"] in (0, 512, 1024, 2048) and res["scatter_mode"] in (0, 1) and res["ms_per_pass"] > 0
-    assert res["adj_tile_nodes"] in (512, 1024, 2048) and res["gather_tile_nodes"] in (1024, 2048, 2816)
+    assert res["adj_tile_nodes"] in (0, 512, 1024, 2048) and res["gather_tile_nodes"] in (1024, 2048, 2816)
     assert res["block_threads"] in (128, 256)
     assert cg.get_tuning() == {k: res[k] for k in ("tile_nodes", "scatter_mode", "adj_tile_nodes",
                                                    "gather_tile_nodes", "block_threads")}
