@@ -255,7 +255,13 @@ def run_ours(args, rank, world, device):
     cg.set_stream(stream)
     tgt = torch.tensor(w.target, dtype=torch.float32, device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
-    if args.no_autotune:
+    if args.tiles:
+        # fixed tile budgets (P2G, G2P transpose, P2G-transpose gather), e.g.
+        # the ones the autotuner picked for a full run, for profiler captures
+        tp, ta, tg = (int(v) for v in args.tiles.split(","))
+        cg.set_tuning(tp, 1, ta, tg)
+        tuning = cg.get_tuning()
+    elif args.no_autotune:
         tuning = cg.get_tuning()
     else:
         # tune from the stored layer halfway through a computed rollout: its
@@ -270,6 +276,8 @@ def run_ours(args, rank, world, device):
     torch.cuda.synchronize(device)
 
     # ---- timed region (device-resident inputs)
+    if args.profile_window:
+        torch.cuda.profiler.start()  # an external profiler started with capture off begins here
     lib.mpm_profile_reset()
     lib.mpm_profile_enable(1)
     launches0 = lib.mpm_launch_count()
@@ -289,9 +297,11 @@ def run_ours(args, rank, world, device):
     barrier(world)
     launches = lib.mpm_launch_count() - launches0
     lib.mpm_profile_enable(0)
+    if args.profile_window:
+        torch.cuda.profiler.stop()
     kern = {}
     import ctypes as C
-    for k in range(11):
+    for k in range(13):
         cnt, ms = C.c_longlong(), C.c_double()
         lib.mpm_profile_query(k, C.byref(cnt), C.byref(ms))
         if cnt.value:
@@ -796,6 +806,9 @@ def main():
                     help="override the workload's checkpoint interval (1: full tape, no recomputation)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--profile-window", action="store_true",
+                    help="start/stop an external profiler around the timed steps (ncu --profile-from-start off)")
+    ap.add_argument("--tiles", default="", help="P2G,G2P-transpose,gather tile budgets instead of the autotuner")
     ap.add_argument("--deterministic", action="store_true",
                     help="fixed-point node sums (bitwise reproducible passes)")
     ap.add_argument("--no-det", action="store_true", help="morph500k: float atomics instead of fixed point")

@@ -119,7 +119,8 @@ void mpm_default_params(mpm_params* p);
 void mpm_default_options(mpm_options* o);
 /* progress messages like the reference's std::cout lines (1 = on, default) */
 void mpm_set_verbose(int verbose);
-/* shared-memory node-tile budget of the scatter kernels (0 disables tiles) */
+/* shared-memory node-tile budget of the scatter kernels (0, the default:
+ * no tile, each cell group's sums go to global memory as float4 reductions) */
 int mpm_set_tile_nodes(int nodes);
 /* FP32 scatter strategy of P2G and the G2P transpose: 1 = segmented (one
  * warp per run of particles sharing a cell, one lane per stencil node; the
@@ -280,8 +281,10 @@ int mpm_constitutive(int n, int precision, int material, int adjoint, const doub
 /* kernel ids for the profiler */
 enum { MPM_K_P2G = 0, MPM_K_GRID_UPDATE = 1, MPM_K_G2P = 2, MPM_K_G2P_ADJ = 3, MPM_K_GRID_ADJ = 4,
        MPM_K_P2G_ADJ = 5, MPM_K_LOSS = 6, MPM_K_ADAM = 7, MPM_K_NORM = 8,
-       MPM_K_G2P2G = 10, /* G2P of a step fused with the next step's P2G */
-       MPM_K_COUNT = 11 };
+       MPM_K_G2P2G = 10,    /* G2P of a step fused with the next step's P2G */
+       MPM_K_RESORT = 11,   /* in-rollout re-sort at a segment start (sort, gathers) */
+       MPM_K_BOUNDARY = 12, /* backward pass: gradients carried across a re-sorted boundary */
+       MPM_K_COUNT = 13 };
 /* record CUDA events around every kernel launch on its stream (1 = on) */
 int mpm_profile_enable(int on);
 int mpm_profile_reset(void);
@@ -297,14 +300,14 @@ int mpm_compgraph_set_tuning(mpm_compgraph* cg, int tile_nodes, int scatter_mode
 int mpm_compgraph_get_tuning(const mpm_compgraph* cg, int* tile_nodes, int* scatter_mode);
 /* node-tile budgets of the adjoint kernels (FP32): the G2P transpose's
  * scatter and the P2G transpose's gather, whose best sizes differ from P2G's
- * (-1: follow the set_tuning budget, the default; 0..2816 nodes); get
- * returns the budgets in effect */
+ * (-1, the default: the scatter follows the set_tuning budget, the gather
+ * stages 2048 nodes; 0..2816 nodes); get returns the budgets in effect */
 int mpm_compgraph_set_adjoint_tiles(mpm_compgraph* cg, int scatter_nodes, int gather_nodes);
 /* No counterpart in the reference: threads per block of the step kernels
- * (P2G, the fused G2P->P2G, G2P and the two adjoint kernels), 128 or 256
- * (-1: 256, the default).  Each thread takes one particle, so this is also
- * the particles per block; the segmented scatter's node tile covers one
- * block's particles. */
+ * (P2G, the fused G2P->P2G, G2P and the G2P transpose; the P2G transpose
+ * keeps 256), 128 or 256 (-1: 256, the default).  Each thread takes one
+ * particle, so this is also the particles per block; the segmented
+ * scatter's node tile covers one block's particles. */
 int mpm_compgraph_set_block_threads(mpm_compgraph* cg, int threads);
 int mpm_compgraph_get_block_threads(const mpm_compgraph* cg, int* threads);
 int mpm_compgraph_get_adjoint_tiles(const mpm_compgraph* cg, int* scatter_nodes, int* gather_nodes);

@@ -43,7 +43,10 @@ namespace mpm {
 #define MPM_FUSE_G2P2G 1
 #endif
 
-int g_tile_nodes = 2048;
+// scatter tiles off by default: the cell-group sums go straight to global
+// memory as float4 reductions, faster than a shared tile and its flush on
+// every workload measured; the gather tile has its own default
+int g_tile_nodes = 0;
 int g_scatter_mode = 1;
 int g_fuse_steps = 1;
 long long g_launches = 0;
@@ -465,13 +468,37 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
         }
     }
     if (blockwide) __syncthreads();
-    // 4. each warp walks its runs; lane owns stencil nodes lane and lane+32
+    // 4. each warp walks its cell groups, summing each group's contributions
+    //    to the nodes a lane owns in registers, then deposits the sums
+    const float* wrec = recs + (size_t)(warp * 32) * kRec;
+    auto deposit = [&](int i, int j, int k, const float* acc) {
+        if constexpr (DET) {
+            if (tile) {
+                const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
+#pragma unroll
+                for (int q = 0; q < NC; ++q)
+                    if (acc[q] != 0.f) atomicAdd(&tilefix[q * vol + idx], to_fix(acc[q], scale[q], ovf));
+            } else if (in_grid(kp, i, j, k)) {
+                const long long nd = node_of(kp, i, j, k);
+#pragma unroll
+                for (int q = 0; q < NC; ++q)
+                    if (acc[q] != 0.f) atomicAdd(&fx->acc[nd * 4 + q], to_fix(acc[q], scale[q], ovf));
+            }
+        } else if (tile) {
+            const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
+#pragma unroll
+            for (int q = 0; q < NC; ++q)
+                if (acc[q] != 0.f) atomicAdd(&tilebuf[q * vol + idx], acc[q]);
+        } else if (in_grid(kp, i, j, k)) {
+            add_node<NC>(grid + node_of(kp, i, j, k) * 4, acc);
+        }
+    };
+    // a lane owns stencil nodes lane and lane+32
     constexpr int NODES = K * K * K;
     const int n0 = lane, n1 = lane + 32;
     const int a0 = n0 / (K * K), bb = (n0 / K) % K, cc = n0 % K;
     const bool has0 = n0 < NODES, has1 = n1 < NODES;
     const int a1 = has1 ? n1 / (K * K) : 0;
-    const float* wrec = recs + (size_t)(warp * 32) * kRec;
     while (todo) {
         const int lead = __ffs(todo) - 1;
         const unsigned members = __shfl_sync(0xffffffffu, grp, lead);
@@ -518,32 +545,8 @@ __device__ void seg_scatter(const KP<float>& kp, bool valid, const Stencil<float
                     if (NC == 4) acc1[NC - 1] += w * q0.w;
                 }
             }
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (h == 1 && !has1) break;
-                const float* acc = h == 0 ? acc0 : acc1;
-                const int i = i0 + (h == 0 ? a0 : a1), j = j0 + bb, k = k0 + cc;
-                if constexpr (DET) {
-                    if (tile) {
-                        const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
-#pragma unroll
-                        for (int q = 0; q < NC; ++q)
-                            if (acc[q] != 0.f) atomicAdd(&tilefix[q * vol + idx], to_fix(acc[q], scale[q], ovf));
-                    } else if (in_grid(kp, i, j, k)) {
-                        const long long nd = node_of(kp, i, j, k);
-#pragma unroll
-                        for (int q = 0; q < NC; ++q)
-                            if (acc[q] != 0.f) atomicAdd(&fx->acc[nd * 4 + q], to_fix(acc[q], scale[q], ovf));
-                    }
-                } else if (tile) {
-                    const int idx = ((i - b0) * e1 + (j - b1)) * e2 + (k - b2);
-#pragma unroll
-                    for (int q = 0; q < NC; ++q)
-                        if (acc[q] != 0.f) atomicAdd(&tilebuf[q * vol + idx], acc[q]);
-                } else if (in_grid(kp, i, j, k)) {
-                    add_node<NC>(grid + node_of(kp, i, j, k) * 4, acc);
-                }
-            }
+            deposit(i0 + a0, j0 + bb, k0 + cc, acc0);
+            if (has1) deposit(i0 + a1, j0 + bb, k0 + cc, acc1);
         }
     }
     if (blockwide) __syncthreads();
@@ -1926,8 +1929,8 @@ int tile_cap_for(const StepCfg& c)
     return sizeof(R) == 4 ? (c.tile_nodes >= 0 ? c.tile_nodes : g_tile_nodes) : 0;
 }
 
-// the G2P transpose's scatter tile and the P2G transpose's gather tile:
-// their own budgets when the graph sets them, else P2G's
+// the G2P transpose's scatter tile: its own budget when the graph sets it,
+// else P2G's; the P2G transpose's gather tile: its own budget, else 2048
 template <typename R>
 int adj_cap_for(const StepCfg& c)
 {
@@ -1937,7 +1940,8 @@ int adj_cap_for(const StepCfg& c)
 template <typename R>
 int gather_cap_for(const StepCfg& c)
 {
-    return sizeof(R) == 4 && c.gather_tile_nodes >= 0 ? c.gather_tile_nodes : tile_cap_for<R>(c);
+    if (sizeof(R) != 4) return 0;
+    return c.gather_tile_nodes >= 0 ? c.gather_tile_nodes : kGatherTileDefault;
 }
 
 inline int scatter_mode_of(const StepCfg& c) { return c.scatter_mode >= 0 ? c.scatter_mode : g_scatter_mode; }
@@ -2170,7 +2174,10 @@ void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
                     const R* g1, const R* trust, const R* grid, const R* adj, R* g, R* gFt, R* glam, R* gmu,
                     cudaStream_t s)
 {
-    const int T = c.threads == 128 ? 128 : kThreads;
+    // 256 threads whatever the graph's block size: at its 255 registers two
+    // 128-thread blocks per SM ran slower (0.579 against 0.532 ms per launch
+    // on 2M particles)
+    const int T = kThreads;
     if (n <= 0) return;
     auto kp = make_kp<R>(c);
     const int cap = gather_cap_for<R>(c);

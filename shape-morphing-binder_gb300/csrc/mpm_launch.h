@@ -83,6 +83,8 @@ size_t inst_table_bytes(int count, int prec_bytes);
 
 // Shared-memory tile budget (nodes) for the scatter kernels; 0 disables tiles.
 extern int g_tile_nodes;
+// nodes the P2G transpose stages per block unless the graph sets its budget
+constexpr int kGatherTileDefault = 2048;
 // FP32 scatter strategy: 1 = segmented (warp per cell segment, lane per
 // node), 0 = per-particle scatter
 extern int g_scatter_mode;

@@ -104,14 +104,14 @@ def test_scatter_strategies_agree(dm, mode, tile):
     prm = O.Params(dt=1e-3, drag=0.0, smoothing=0.0, exact=True)
     seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
     lib = dm._lib.lib
-    xb, gb, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")  # defaults: segmented + tile 2048
+    xb, gb, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")  # defaults: segmented, no tile
     try:
         lib.mpm_set_scatter_mode(mode)
         lib.mpm_set_tile_nodes(tile)
         xa, ga, _, _ = _rollout(dm, s0, g, prm, 3, seed_gx, "fp32")
     finally:
         lib.mpm_set_scatter_mode(1)
-        lib.mpm_set_tile_nodes(2048)
+        lib.mpm_set_tile_nodes(0)
     assert rel_err(xa, xb) < 1e-6
     for k in ("x", "v", "F"):
         assert norm_err(ga[k], gb[k]) < 1e-4, k
@@ -393,7 +393,7 @@ def test_adjoint_tile_budgets_change_no_result(dm):
                               deterministic=True)
         cg.set_tuning(1024, 1, at, gt)
         tun = cg.get_tuning()
-        assert (tun["adj_tile_nodes"], tun["gather_tile_nodes"]) == (1024 if at < 0 else at, 1024 if gt < 0 else gt)
+        assert (tun["adj_tile_nodes"], tun["gather_tile_nodes"]) == (1024 if at < 0 else at, 2048 if gt < 0 else gt)
         cg.compute_forward_pass(0, 0)
         last = cg.get_point_cloud(T)
         last.set("grad_x", seed)
