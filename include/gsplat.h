@@ -53,6 +53,13 @@ typedef struct GsScene {
     const float* cov3D;         /* (P,6) precomputed (xx,xy,xz,yy,yz,zz) or NULL (then scales/rotations) */
     const float* norm3D;        /* (P,3) precomputed normals or NULL (then from scales/rotations) */
     const float* extra;         /* (P,extra_dims) or NULL */
+    /* 0: the reference's gradients (the default of the Python module): the
+     * rotation gradient through a normal taken from scales/rotations carries
+     * the sign backward.cu:364-366 gives it, which tests a row of the
+     * rotation matrix where the forward pass took a column (forward.cu:188),
+     * so for some Gaussians it is the negated derivative; 1: the exact
+     * derivative of the forward pass.  Everything else is the same. */
+    int exact_adjoint;
 } GsScene;
 
 /* per-Gaussian results of gs_preprocess (caller-allocated, P entries each) */

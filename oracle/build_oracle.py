@@ -11,6 +11,8 @@
   ``public:`` edit (so ``ref_driver.cpp`` can set CompGraph's dt, drag and
   smoothing) are applied to temporary copies outside this repository.  Only
   the two shared libraries are written into ``oracle/_ref/``.
+* ``oracle/_ref/gs_*.cubin`` -- the reference's Gaussian rasterizer kernels
+  (``build_ref_gauss``), from the same checkout.
 
 Usage: ``REF_DIR=<reference checkout> python oracle/build_oracle.py [--no-ref] [--force]``
 """
@@ -133,6 +135,42 @@ def build_ref(force: bool = False) -> list[Path]:
     return outs
 
 
+GAUSS_SUBDIR = Path("gaussian-splatting") / "submodules" / "diff-gaussian-rasterization"
+GAUSS_UNITS = {"gs_forward.cubin": "forward.cu", "gs_backward.cubin": "backward.cu",
+               "gs_impl.cubin": "rasterizer_impl.cu"}
+
+
+def build_ref_gauss(force: bool = False) -> list[Path]:
+    """The reference's differentiable Gaussian rasterizer
+    (``cuda_rasterizer/{forward,backward,rasterizer_impl}.cu``) compiled as
+    sm_103a device code (cubins) into ``oracle/_ref/``, from the sources
+    where they lie (``-include cstdint``: rasterizer_impl.h uses uint32_t
+    without including it; its own build gets it through torch's headers).
+    Device code does not depend on the host's architecture, so the cubins
+    run on the GPU host, driven by ``tests/golden/make_gauss_golden.py``."""
+    ref = ref_dir()
+    if ref is None:
+        return []
+    src = ref / GAUSS_SUBDIR
+    if not (src / "cuda_rasterizer" / "forward.cu").exists():
+        return []
+    OUT_REF.mkdir(exist_ok=True)
+    nvcc = os.environ.get("NVCC") or "/usr/local/cuda/bin/nvcc"
+    headers = list((src / "cuda_rasterizer").glob("*.h"))
+    outs, jobs = [], []
+    for name, unit in GAUSS_UNITS.items():
+        out = OUT_REF / name
+        outs.append(out)
+        cu = src / "cuda_rasterizer" / unit
+        if force or not _newer(out, [cu, Path(__file__), *headers]):
+            jobs.append([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                         "-include", "cstdint", "-I", str(src / "third_party" / "glm"),
+                         "-I", str(src / "cuda_rasterizer"), "-w", str(cu), "-o", str(out)])
+    with cf.ThreadPoolExecutor(max_workers=len(jobs) or 1) as ex:
+        list(ex.map(_compile, [(j,) for j in jobs]))
+    return outs
+
+
 def build_ref_module(widen: bool = False, force: bool = False) -> Path | None:
     """The reference's own Python module, ``diffmpm_bindings`` (bind/bind.cpp
     and the DiffMPMLib3D sources, without its optional torch support),
@@ -182,7 +220,7 @@ def main() -> int:
     a = ap.parse_args()
     print(build_oracle(a.force))
     if not a.no_ref:
-        for p in build_ref(a.force):
+        for p in build_ref(a.force) + build_ref_gauss(a.force):
             print(p)
     return 0
 

@@ -78,7 +78,7 @@ __device__ __forceinline__ void quat_rot(const float* q, float* R)
 }
 
 // normal axis of a Gaussian: the local axis of smallest scale (ties as the
-// reference's branch order), as a row of R
+// reference's branch order), as a column of R
 __device__ __forceinline__ int normal_axis(const float* s)
 {
     if (s[0] > s[2] && s[1] > s[2]) return 2;
@@ -227,8 +227,11 @@ __global__ void k_gs_preprocess(Frame f, GsScene s, GsGeom g)
     } else {
         float R[9], Mx[9];
         quat_rot(s.rotations + 4 * i, R);
+        // M = S R^T: glm::mat3's constructor takes the quaternion matrix's
+        // rows as columns (forward.cu:134-140), so the reference's Sigma is
+        // R S^2 R^T with R as quat_rot writes it
         for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) Mx[3 * r + c] = f.mod * s.scales[3 * i + r] * R[3 * r + c];
+            for (int c = 0; c < 3; ++c) Mx[3 * r + c] = f.mod * s.scales[3 * i + r] * R[3 * c + r];
         // Sigma = M^T M
         c6[0] = Mx[0] * Mx[0] + Mx[3] * Mx[3] + Mx[6] * Mx[6];
         c6[1] = Mx[0] * Mx[1] + Mx[3] * Mx[4] + Mx[6] * Mx[7];
@@ -245,7 +248,8 @@ __global__ void k_gs_preprocess(Frame f, GsScene s, GsGeom g)
         float R[9];
         quat_rot(s.rotations + 4 * i, R);
         const int a = normal_axis(s.scales + 3 * i);
-        nrm = v3(R[3 * a], R[3 * a + 1], R[3 * a + 2]);
+        // column a of R (transpose(R_glm) * e_a, forward.cu:188)
+        nrm = v3(R[a], R[3 + a], R[6 + a]);
         const V3 ray = v3(m.x - s.campos[0], m.y - s.campos[1], m.z - s.campos[2]);
         if (ray.x * nrm.x + ray.y * nrm.y + ray.z * nrm.z > 0.f) nrm = v3(-nrm.x, -nrm.y, -nrm.z);
     }
@@ -684,7 +688,7 @@ __global__ void k_gs_preprocess_bwd(Frame f, GsScene s, GsGeom g, GsGrads gr)
         dm[2] += (gdir[2] - d.z * dd) * il;
     }
     for (int k = 0; k < 3; ++k) gr.means3D[3 * i + k] = dm[k];
-    // 5. scale/rotation: Sigma = M^T M, M = S R; the normal is a signed row of R
+    // 5. scale/rotation: Sigma = M^T M, M = S R^T; the normal is a signed column of R
     if (s.scales && s.rotations && (gr.scales || gr.rotations) && (!s.cov3D || !s.norm3D)) {
         const float* q = s.rotations + 4 * i;
         const float* sc = s.scales + 3 * i;
@@ -693,24 +697,30 @@ __global__ void k_gs_preprocess_bwd(Frame f, GsScene s, GsGeom g, GsGrads gr)
         if (!s.cov3D) {
             float Mx[9], dM[9];
             for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) Mx[3 * r + c] = f.mod * sc[r] * R[3 * r + c];
+                for (int c = 0; c < 3; ++c) Mx[3 * r + c] = f.mod * sc[r] * R[3 * c + r];
             // dL/dM = 2 M dS (dS symmetric)
             for (int r = 0; r < 3; ++r)
                 for (int c = 0; c < 3; ++c)
                     dM[3 * r + c] = 2.f * (Mx[3 * r] * dS[c] + Mx[3 * r + 1] * dS[3 + c] + Mx[3 * r + 2] * dS[6 + c]);
+            // M[r][c] = mod s_r R[c][r]
             for (int r = 0; r < 3; ++r) {
-                dsc[r] = f.mod * (dM[3 * r] * R[3 * r] + dM[3 * r + 1] * R[3 * r + 1] + dM[3 * r + 2] * R[3 * r + 2]);
-                for (int c = 0; c < 3; ++c) dR[3 * r + c] = dM[3 * r + c] * f.mod * sc[r];
+                dsc[r] = f.mod * (dM[3 * r] * R[r] + dM[3 * r + 1] * R[3 + r] + dM[3 * r + 2] * R[6 + r]);
+                for (int c = 0; c < 3; ++c) dR[3 * c + r] = dM[3 * r + c] * f.mod * sc[r];
             }
         }
         if (gr.scales)
             for (int r = 0; r < 3; ++r) gr.scales[3 * i + r] = dsc[r];
         if (!s.norm3D) {
             const int a = normal_axis(sc);
-            // the stored normal is +/- row a of R
-            const float sgn = (g.normal[3 * i] * R[3 * a] + g.normal[3 * i + 1] * R[3 * a + 1] +
-                               g.normal[3 * i + 2] * R[3 * a + 2]) < 0.f ? -1.f : 1.f;
-            for (int c = 0; c < 3; ++c) dR[3 * a + c] += sgn * gr.norm3D[3 * i + c];
+            // the stored normal is +/- column a of R; the exact adjoint takes
+            // that sign, the reference's backward (backward.cu:364-366) the
+            // sign of the stored normal against row a
+            const float b0 = s.exact_adjoint ? R[a] : R[3 * a], b1 = s.exact_adjoint ? R[3 + a] : R[3 * a + 1],
+                        b2 = s.exact_adjoint ? R[6 + a] : R[3 * a + 2];
+            const float sgn = (g.normal[3 * i] * b0 + g.normal[3 * i + 1] * b1 + g.normal[3 * i + 2] * b2) < 0.f
+                                  ? -1.f
+                                  : 1.f;
+            for (int c = 0; c < 3; ++c) dR[3 * c + a] += sgn * gr.norm3D[3 * i + c];
         }
         if (!gr.rotations) return;
         const float r = q[0], x = q[1], y = q[2], z = q[3];

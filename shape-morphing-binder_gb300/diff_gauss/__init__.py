@@ -27,12 +27,27 @@ GS_TILE = 16
 GS_MAX_EXTRA = 34
 
 
+# gradients: the reference's (default) or the exact derivative of the forward
+# pass; they differ only in the rotation gradient through normals taken from
+# scales and rotations (include/gsplat.h, GsScene.exact_adjoint)
+_ADJOINT = {"exact": 0}
+
+
+def set_adjoint(mode: str = "reference") -> None:
+    """'reference': the reference rasterizer's gradients, including the sign
+    its backward gives the rotation gradient through the normal (additive;
+    the default); 'exact': the derivative of the forward pass."""
+    if mode not in ("reference", "exact"):
+        raise ValueError("adjoint must be 'reference' or 'exact'")
+    _ADJOINT["exact"] = int(mode == "exact")
+
+
 class _Scene(C.Structure):
     _fields_ = [("P", C.c_int), ("H", C.c_int), ("W", C.c_int), ("tanfovx", C.c_float), ("tanfovy", C.c_float),
                 ("scale_modifier", C.c_float), ("sh_degree", C.c_int), ("sh_coeffs", C.c_int),
                 ("extra_dims", C.c_int), ("bg", _vp), ("viewmatrix", _vp), ("projmatrix", _vp), ("campos", _vp),
                 ("means3D", _vp), ("opacities", _vp), ("shs", _vp), ("colors", _vp), ("scales", _vp),
-                ("rotations", _vp), ("cov3D", _vp), ("norm3D", _vp), ("extra", _vp)]
+                ("rotations", _vp), ("cov3D", _vp), ("norm3D", _vp), ("extra", _vp), ("exact_adjoint", C.c_int)]
 
 
 class _Geom(C.Structure):
@@ -93,6 +108,7 @@ def _scene(s: GaussianRasterizationSettings, means3D, opacities, sh, colors, sca
     sc.means3D, sc.opacities, sc.shs, sc.colors = _ptr(t["means3D"]), _ptr(t["opacities"]), _ptr(t["sh"]), _ptr(t["colors"])
     sc.scales, sc.rotations, sc.cov3D = _ptr(t["scales"]), _ptr(t["rotations"]), _ptr(t["cov3D"])
     sc.norm3D, sc.extra = _ptr(t["norm3D"]), _ptr(t["extra"])
+    sc.exact_adjoint = _ADJOINT["exact"]
     return sc
 
 

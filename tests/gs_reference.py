@@ -68,7 +68,9 @@ def render(means3D, opacities, H, W, tanfovx, tanfovy, bg, view, proj, campos, *
                         1).reshape(-1, 3, 3)
     else:
         R = quat_rot(rotations.to(dt))
-        M = (scale_modifier * scales.to(dt))[:, :, None] * R
+        # Sigma = R S^2 R^T (M = S R^T): glm::mat3's constructor takes the
+        # rows written in forward.cu:134-140 as columns
+        M = (scale_modifier * scales.to(dt))[:, :, None] * R.transpose(1, 2)
         S = M.transpose(1, 2) @ M
     if norm3D is not None:
         nrm = norm3D.to(dt)
@@ -77,7 +79,7 @@ def render(means3D, opacities, H, W, tanfovx, tanfovy, bg, view, proj, campos, *
         s = scales
         axis = torch.where((s[:, 0] > s[:, 2]) & (s[:, 1] > s[:, 2]), 2,
                            torch.where((s[:, 0] > s[:, 1]) & (s[:, 2] > s[:, 1]), 1, 0))
-        nrm = R[torch.arange(P), axis]
+        nrm = R[torch.arange(P), :, axis]  # column: transpose(R_glm) * e_axis, forward.cu:188
         ray = m - campos.to(dt)
         flip = ((ray * nrm).sum(1) > 0).to(dt)
         nrm = nrm * (1 - 2 * flip)[:, None]
