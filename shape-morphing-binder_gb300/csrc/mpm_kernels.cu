@@ -752,9 +752,11 @@ __device__ GTile stage_gather_tile(const KP<float>& kp, bool valid, const int* b
             g.e1 = (int)x1;
             g.e2 = (int)x2;
             const int vol = (int)(x0 * x1 * x2);
+            // u / e by a multiply-high: e >= K > 1 and u < 2^20 keep it exact
+            const unsigned m2 = 0xFFFFFFFFu / (unsigned)g.e2 + 1u, m1 = 0xFFFFFFFFu / (unsigned)g.e1 + 1u;
             for (int u = t; u < vol; u += blockDim.x) {
-                const int kk = u % g.e2, rr = u / g.e2;
-                const int jj = rr % g.e1, ii = rr / g.e1;
+                const int rr = (int)__umulhi((unsigned)u, m2), kk = u - rr * g.e2;
+                const int ii = (int)__umulhi((unsigned)rr, m1), jj = rr - ii * g.e1;
                 const int i = g.b0 + ii, j = g.b1 + jj, k = g.b2 + kk;
                 float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
                 if (in_grid(kp, i, j, k)) {
@@ -1874,15 +1876,16 @@ __global__ void k_planes_to_aos(int n, int k, long long ld, const R* __restrict_
     dst[row * k + q] = (T)src[(long long)q * ld + p];
 }
 
-// dst slot i <- src slot order[i], plane by plane (the re-sort)
+// dst slot i <- src slot order[i], plane by plane (the re-sort); one grid
+// row per plane
 template <typename R>
-__global__ void k_gather_planes(int n, int k, long long ld, const int* __restrict__ order, const R* __restrict__ src,
+__global__ void k_gather_planes(int n, long long ld, const int* __restrict__ order, const R* __restrict__ src,
                                 R* __restrict__ dst)
 {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)n * k) return;
-    const int i = (int)(t % n), q = (int)(t / n);
-    dst[(long long)q * ld + i] = src[(long long)q * ld + order[i]];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long q = blockIdx.y;
+    dst[q * ld + i] = src[q * ld + order[i]];
 }
 
 template <typename R>
@@ -2314,7 +2317,8 @@ void launch_gather_planes(int n, int k, long long ld, const int* order, const R*
 {
     if (n <= 0) return;
     counted();
-    k_gather_planes<R><<<nblocks((long long)n * k), kThreads, 0, s>>>(n, k, ld, order, src, dst);
+    if (k <= 0) return;
+    k_gather_planes<R><<<dim3(nblocks(n), k), kThreads, 0, s>>>(n, ld, order, src, dst);
 }
 
 template <typename R>
