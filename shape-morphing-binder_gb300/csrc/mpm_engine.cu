@@ -539,6 +539,11 @@ struct Graph {
     cudaStream_t own = nullptr, stream = nullptr;
     // scratch
     Buf adj, lgm, ldm, acc;
+    // the backward steps use adj and adj2 in turn: a step's grid adjoint
+    // clears the other one for the next step (adj_flip: adj2 is current;
+    // adj_clear: the current one is known zero)
+    Buf adj2;
+    bool adj_flip = false, adj_clear = false;
     Buf fgrid, fgrid2, ftrust;                      // checkpointed forward (two grids: fused steps)
     std::shared_ptr<PCData> ping, pong;             // non-stored forward states
     std::vector<std::shared_ptr<PCData>> seg;       // recomputed segment states
@@ -891,6 +896,11 @@ void run_forward_steps(const StepCfg& c, const std::vector<StepBufs>& plan, cuda
         ensure(g, sizeof(R) * 4 * nn, s, false);
         ck(cudaMemsetAsync(g->p, 0, sizeof(R) * 4 * nn, s), "grid reset");
     };
+    // the grid update of step k clears step k+1's grid (a distinct buffer)
+    auto next_grid = [&](int k) -> R* {
+        if (!MPM_FUSE_CLEAR || k + 1 >= m) return nullptr;
+        return ensure(*plan[k + 1].grid, sizeof(R) * 4 * nn, s, false)->template as<R>();
+    };
     // the first step's P2G on its own
     {
         PCData& a = *plan[0].a;
@@ -906,8 +916,9 @@ void run_forward_steps(const StepCfg& c, const std::vector<StepBufs>& plan, cuda
         PCData& a = *st.a;
         PCData& b = *st.b;
         {
+            R* zn = next_grid(k);
             KTimer kt(K_GRID_UPDATE, s);
-            launch_grid_update<R>(c, (*st.grid)->as<R>(), s);
+            launch_grid_update<R>(c, (*st.grid)->as<R>(), s, zn);
         }
         check_launch("grid_update");
         const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
@@ -915,7 +926,7 @@ void run_forward_steps(const StepCfg& c, const std::vector<StepBufs>& plan, cuda
         if (c.exact) tr = ensure(*st.trust, sizeof(R) * a.ld, s, false)->as<R>();
         if (!b.st) b.st = make_buf(a.planes_bytes(ST_N), s, false);
         if (k + 1 < m) {
-            prep_grid(*plan[k + 1].grid);
+            if (!MPM_FUSE_CLEAR) prep_grid(*plan[k + 1].grid);
             KTimer kt(K_G2P2G, s);
             if constexpr (sizeof(R) == 4)
                 launch_g2p2g(c, a.n, a.ld, a.st->as<float>(), dfc, a.co->as<float>(), (*st.grid)->as<float>(),
@@ -938,20 +949,24 @@ void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& 
     ++g_bwd_steps;
     const long long nn = c.nodes();
     if (!grid) fail(MPM_ERR_STATE, "backward pass before the forward pass of this step");
-    ensure(G.adj, sizeof(R) * 4 * nn, s, false);
-    if (!c.det()) ck(cudaMemsetAsync(G.adj->p, 0, sizeof(R) * 4 * nn, s), "adj reset");
+    Buf& adj = G.adj_flip ? G.adj2 : G.adj;
+    Buf& adj_next = G.adj_flip ? G.adj : G.adj2;
+    ensure(adj, sizeof(R) * 4 * nn, s, false);
+    if (!c.det() && !G.adj_clear) ck(cudaMemsetAsync(adj->p, 0, sizeof(R) * 4 * nn, s), "adj reset");
     ensure_grads(a, s);
     ensure_grads(b, s);
     const R* dfc = a.dfc_zero ? nullptr : a.dfc->as<R>();
     const R* tr = (c.exact && trust) ? trust->as<R>() : nullptr;
     {
         KTimer kt(K_G2P_ADJ, s);
-        launch_g2p_adj<R>(c, a.n, a.ld, a.st->as<R>(), dfc, b.st->as<R>(), b.grads->as<R>(), tr, G.adj->as<R>(), s);
+        launch_g2p_adj<R>(c, a.n, a.ld, a.st->as<R>(), dfc, b.st->as<R>(), b.grads->as<R>(), tr, adj->as<R>(), s);
     }
     check_launch("g2p_adj");
     {
         KTimer kt(K_GRID_ADJ, s);
-        launch_grid_adj<R>(c, grid->as<R>(), G.adj->as<R>(), s);
+        R* zn = (MPM_FUSE_CLEAR && !c.det()) ? ensure(adj_next, sizeof(R) * 4 * nn, s, false)->as<R>() : nullptr;
+        launch_grid_adj<R>(c, grid->as<R>(), adj->as<R>(), s, zn);
+        G.adj_clear = zn != nullptr;
     }
     check_launch("grid_adj");
     R* gctl = nullptr;
@@ -965,9 +980,10 @@ void step_backward(Graph& G, const StepCfg& c, PCData& a, PCData& b, const Buf& 
     {
         KTimer kt(K_P2G_ADJ, s);
         launch_p2g_adj<R>(c, a.n, a.ld, a.st->as<R>(), dfc, a.co->as<R>(), b.st->as<R>(), b.grads->as<R>(), tr,
-                          grid->as<R>(), G.adj->as<R>(), a.grads->as<R>(), gctl, glam, gmu, s);
+                          grid->as<R>(), adj->as<R>(), a.grads->as<R>(), gctl, glam, gmu, s);
     }
     check_launch("p2g_adj");
+    G.adj_flip = !G.adj_flip;
 }
 
 std::shared_ptr<PCData> shell_like(const PCData& a, cudaStream_t s, bool with_state)
@@ -1468,6 +1484,7 @@ void graph_backward(Graph& G, int control)
         sig.add(G.rs_tmp);
     }
     sig.add(G.adj);
+    sig.add(G.adj2);
     sig.add((unsigned long long)G.lame_on);
     sig.add(G.glame);
     sig.add_pc(G.ping.get());
@@ -1485,6 +1502,7 @@ void graph_backward(Graph& G, int control)
     run_captured(G, "bwd" + std::to_string(control), sig, [&]() {
         if (G.lame_on) ck(cudaMemsetAsync(G.glame->p, 0, G.glame->bytes, s), "memset");
         begin_fix_pass(G, c, *G.layers[control].pc, s);
+        G.adj_flip = G.adj_clear = false;  // the first step clears its adjoint grid
         if (k == 1) {
             for (int i = L - 2; i >= control; --i) {
                 Layer& la = G.layers[i];

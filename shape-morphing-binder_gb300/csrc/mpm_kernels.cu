@@ -647,10 +647,28 @@ __global__ void __launch_bounds__(kThreads) k_p2g(KP<R> kp, int n, long long ld,
 // -------------------------------------------------------- grid update
 
 template <typename R>
-__global__ void k_grid_update(KP<R> kp, long long nn, R* __restrict__ grid)
+__global__ void k_grid_update(KP<R> kp, long long nn, R* __restrict__ grid, R* __restrict__ zero_next)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
+    if constexpr (sizeof(R) == 4) {
+        // the next step's grid, cleared here instead of by a separate pass
+        if (zero_next) reinterpret_cast<float4*>(zero_next)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // one 16-byte load per node; a node whose update leaves its bits as
+        // they are (every node no particle reached: all zero) is not written
+        float4* g = reinterpret_cast<float4*>(grid) + i;
+        const float4 q = *g;
+        if (q.w > 1e-12f) {
+            *g = make_float4(q.x / q.w + kp.dtf[0], q.y / q.w + kp.dtf[1], q.z / q.w + kp.dtf[2], q.w);
+        } else if ((__float_as_uint(q.x) | __float_as_uint(q.y) | __float_as_uint(q.z)) != 0u || q.w < 0.f) {
+            *g = make_float4(0.f, 0.f, 0.f, q.w < 0.f ? 0.f : q.w);
+        }
+        return;
+    }
+    if (zero_next) {
+        R* z = zero_next + 4 * i;
+        z[0] = z[1] = z[2] = z[3] = R(0);
+    }
     R* g = grid + 4 * i;
     R m = g[3];
     if (m < R(0)) m = R(0);
@@ -1299,10 +1317,37 @@ __global__ void k_grid_adj_fix(KP<float> kp, long long nn, const float* __restri
 
 // G_op^T (BackPropagation.cpp:59-72)
 template <typename R>
-__global__ void k_grid_adj(KP<R> kp, long long nn, const R* __restrict__ grid, R* __restrict__ adj)
+__global__ void k_grid_adj(KP<R> kp, long long nn, const R* __restrict__ grid, R* __restrict__ adj,
+                           R* __restrict__ zero_next)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
+    if (zero_next) {  // the adjoint grid of the next (earlier) step
+        if constexpr (sizeof(R) == 4) reinterpret_cast<float4*>(zero_next)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else {
+            R* z = zero_next + 4 * i;
+            z[0] = z[1] = z[2] = z[3] = R(0);
+        }
+    }
+    if constexpr (sizeof(R) == 4) {
+        // 16-byte accesses; a massless node's adjoint is zeroed unread
+        const float4 q = __ldg(reinterpret_cast<const float4*>(grid) + i);
+        float4* dp = reinterpret_cast<float4*>(adj) + i;
+        if (fabsf(q.w) > 1e-12f) {
+            const float4 dd = *dp;
+            float v0 = q.x, v1 = q.y, v2 = q.z;
+            if (kp.exact) {
+                v0 -= kp.dtf[0];
+                v1 -= kp.dtf[1];
+                v2 -= kp.dtf[2];
+            }
+            const float im = 1.f / q.w;
+            *dp = make_float4(dd.x * im, dd.y * im, dd.z * im, -(v0 * dd.x + v1 * dd.y + v2 * dd.z) * im);
+        } else {
+            *dp = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        return;
+    }
     const R* g = grid + 4 * i;
     R* d = adj + 4 * i;
     const R m = g[3];
@@ -2082,18 +2127,19 @@ void launch_g2p2g(const StepCfg& c, int n, long long ld, const float* st, const 
 }
 
 template <typename R>
-void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s)
+void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s, R* zero_next)
 {
     const long long nn = c.nodes();
     if constexpr (sizeof(R) == 4) {
         if (c.det()) {
+            if (zero_next) cudaMemsetAsync(zero_next, 0, sizeof(R) * 4 * nn, s);
             counted();
             k_grid_update_fix<<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, make_fix(c), grid);
             return;
         }
     }
     counted();
-    k_grid_update<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid);
+    k_grid_update<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, zero_next);
 }
 
 template <typename R>
@@ -2158,18 +2204,19 @@ void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R*
 }
 
 template <typename R>
-void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s)
+void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s, R* zero_next)
 {
     const long long nn = c.nodes();
     if constexpr (sizeof(R) == 4) {
         if (c.det()) {
+            if (zero_next) cudaMemsetAsync(zero_next, 0, sizeof(R) * 4 * nn, s);
             counted();
             k_grid_adj_fix<<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, make_fix(c), adj);
             return;
         }
     }
     counted();
-    k_grid_adj<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, adj);
+    k_grid_adj<R><<<nblocks(nn), kThreads, 0, s>>>(make_kp<R>(c), nn, grid, adj, zero_next);
 }
 
 template <typename R>
@@ -2356,11 +2403,11 @@ void launch_nonfinite(int n, int k, long long ld, const R* y, int* flag, cudaStr
 
 #define MPM_INSTANTIATE(R)                                                                                         \
     template void launch_p2g<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, cudaStream_t);   \
-    template void launch_grid_update<R>(const StepCfg&, R*, cudaStream_t);                                         \
+    template void launch_grid_update<R>(const StepCfg&, R*, cudaStream_t, R*);                                     \
     template void launch_g2p<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, R*, cudaStream_t); \
     template void launch_g2p_adj<R>(const StepCfg&, int, long long, const R*, const R*, const R*, const R*,        \
                                     const R*, R*, cudaStream_t);                                                   \
-    template void launch_grid_adj<R>(const StepCfg&, const R*, R*, cudaStream_t);                                  \
+    template void launch_grid_adj<R>(const StepCfg&, const R*, R*, cudaStream_t, R*);                              \
     template void launch_p2g_adj<R>(const StepCfg&, int, long long, const R*, const R*, const R*, const R*,        \
                                     const R*, const R*, const R*, const R*, R*, R*, R*, R*, cudaStream_t);         \
     template void launch_loss<R>(const StepCfg&, int, long long, const R*, const R*, const R*, R*, R*, double*, R*, \

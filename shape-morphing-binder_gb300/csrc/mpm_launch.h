@@ -12,6 +12,13 @@
 #pragma once
 #include <cuda_runtime.h>
 
+// 1: the grid update of a forward step clears the next step's grid and the
+// grid adjoint of a backward step clears the next adjoint grid, instead of
+// a separate memset pass per step
+#ifndef MPM_FUSE_CLEAR
+#define MPM_FUSE_CLEAR 1
+#endif
+
 namespace mpm {
 
 enum { ST_X = 0, ST_V = 3, ST_C = 6, ST_F = 15, ST_N = 24 };
@@ -97,7 +104,8 @@ template <typename R>
 void launch_p2g(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, R* grid,
                 cudaStream_t s);
 template <typename R>
-void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s);
+// zero_next (or null): a grid of nodes() nodes that the launch also clears
+void launch_grid_update(const StepCfg& c, R* grid, cudaStream_t s, R* zero_next = nullptr);
 template <typename R>
 void launch_g2p(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* grid, R* st1, R* trust,
                 cudaStream_t s);
@@ -113,7 +121,8 @@ template <typename R>
 void launch_g2p_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* st1, const R* g1,
                     const R* trust, R* adj, cudaStream_t s);
 template <typename R>
-void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s);
+// zero_next (or null): an adjoint grid that the launch also clears
+void launch_grid_adj(const StepCfg& c, const R* grid, R* adj, cudaStream_t s, R* zero_next = nullptr);
 template <typename R>
 void launch_p2g_adj(const StepCfg& c, int n, long long ld, const R* st, const R* dfc, const R* co, const R* st1,
                     const R* g1, const R* trust, const R* grid, const R* adj, R* g, R* gFt, R* glam, R* gmu,
