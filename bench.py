@@ -141,9 +141,26 @@ KERNEL_BYTES = {
     "g2p": (148, 16),
     "g2p_adj": (184, 16),
     "p2g_adj": (380, 32),
-    "grid_update": (0, 32),
-    "grid_adj": (0, 48),
+    # the grid kernels also clear the next step's grid (16 B per node)
+    "grid_update": (0, 48),
+    "grid_adj": (0, 64),
 }
+# kernel ids (include/mpm.h): the three largest kernels of a rollout, the
+# candidates for the roofline's kernel
+K_IDS = {"p2g": 0, "grid_update": 1, "g2p": 2, "g2p_adj": 3, "grid_adj": 4, "p2g_adj": 5, "g2p2g": 10}
+ALL_KERNELS = (1 << 13) - 1
+TOP_KERNELS = (1 << K_IDS["p2g_adj"]) | (1 << K_IDS["g2p2g"]) | (1 << K_IDS["g2p_adj"])
+
+
+def query_kernels(lib):
+    import ctypes as C
+    kern = {}
+    for k in range(13):
+        cnt, ms = C.c_longlong(), C.c_double()
+        lib.mpm_profile_query(k, C.byref(cnt), C.byref(ms))
+        if cnt.value:
+            kern[lib.mpm_kernel_name(k).decode()] = (cnt.value, ms.value)
+    return kern
 
 
 def build_graph(dm, w, precision, checkpoint, adjoint="exact", deterministic=False):
@@ -271,6 +288,11 @@ def run_ours(args, rank, world, device):
         mid = (T // 2) // w.checkpoint * w.checkpoint
         tuning = cg.autotune(steps=4, layer=mid)
 
+    # CUDA events around the launches of the selected kernels, on from the
+    # warm-up on: the warm-up rollouts record the passes (with their event
+    # nodes) that the timed rollouts then replay
+    lib.mpm_profile_select(ALL_KERNELS if args.timed_profile == "all" else TOP_KERNELS)
+    lib.mpm_profile_enable(1)
     for _ in range(args.warmup):
         device_rollout(torch, cg, T, tgt, n)
     torch.cuda.synchronize(device)
@@ -279,7 +301,6 @@ def run_ours(args, rank, world, device):
     if args.profile_window:
         torch.cuda.profiler.start()  # an external profiler started with capture off begins here
     lib.mpm_profile_reset()
-    lib.mpm_profile_enable(1)
     launches0 = lib.mpm_launch_count()
     times = []
     barrier(world)
@@ -299,13 +320,18 @@ def run_ours(args, rank, world, device):
     lib.mpm_profile_enable(0)
     if args.profile_window:
         torch.cuda.profiler.stop()
-    kern = {}
-    import ctypes as C
-    for k in range(13):
-        cnt, ms = C.c_longlong(), C.c_double()
-        lib.mpm_profile_query(k, C.byref(cnt), C.byref(ms))
-        if cnt.value:
-            kern[lib.mpm_kernel_name(k).decode()] = (cnt.value, ms.value)
+    kern = query_kernels(lib)
+    kern_all, kern_src = kern, "the timed rollouts"
+    if args.timed_profile == "top":
+        # every kernel timed in one more rollout after the timed region
+        lib.mpm_profile_select(ALL_KERNELS)
+        lib.mpm_profile_reset()
+        lib.mpm_profile_enable(1)
+        device_rollout(torch, cg, T, tgt, n)
+        torch.cuda.synchronize(device)
+        lib.mpm_profile_enable(0)
+        kern_all = {k: (c * args.steps, ms * args.steps) for k, (c, ms) in query_kernels(lib).items()}
+        kern_src = "one untimed rollout after the timed region, scaled to the timed rollouts' count"
     t_total = max_over_ranks(torch, sum(times), world, device)
     value = job_value(world, n * T * args.steps, t_total)
     active = cg.active_nodes(0)
@@ -325,12 +351,13 @@ def run_ours(args, rank, world, device):
         d = json.loads(tp.read_text()).get(top)
         if d and d.get("bytes_per_particle"):
             traffic = d["bytes_per_particle"] * n
-    total_ms = sum(v[1] for v in kern.values())
+    total_ms = sum(v[1] for v in kern_all.values())
     roof = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
             "frac": round(achieved / hbm, 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": traffic, "algorithmic_bytes_per_launch": algo, "launches": cnt,
             "avg_launch_ms": round(ms / cnt, 5),
-            "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(kern.items(), key=lambda x: -x[1][1])}}
+            "kernel_share": {k: round(v[1] / total_ms, 4) for k, v in sorted(kern_all.items(), key=lambda x: -x[1][1])},
+            "timed_kernels": sorted(kern), "kernel_share_source": kern_src}
 
     # ---- e2e through the public API with host buffers
     e2e = None if args.no_e2e else run_e2e(torch, dm, args, w, device, keep, tuning)
@@ -366,7 +393,7 @@ def run_ours(args, rank, world, device):
                    "gradients": "layer 0: x, v, F, C, control F" + (", lam, mu (dL/dE)" if w.extra.get("grad_E")
                                                                     else "")},
         "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
-        "kernels_ms": {k: round(v[1], 3) for k, v in kern.items()}, "active_nodes": active,
+        "kernels_ms": {k: round(v[1], 3) for k, v in kern_all.items()}, "active_nodes": active,
         "native_libs": native_libs(),
     }
     if fp64:
@@ -806,6 +833,9 @@ def main():
                     help="override the workload's checkpoint interval (1: full tape, no recomputation)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--timed-profile", choices=("top", "all"), default="top",
+                    help="kernels with CUDA events in the timed rollouts: the three largest (the roofline's "
+                         "candidates; the full kernel table then comes from one more untimed rollout) or all")
     ap.add_argument("--profile-window", action="store_true",
                     help="start/stop an external profiler around the timed steps (ncu --profile-from-start off)")
     ap.add_argument("--tiles", default="", help="P2G,G2P-transpose,gather tile budgets instead of the autotuner")

@@ -287,6 +287,10 @@ enum { MPM_K_P2G = 0, MPM_K_GRID_UPDATE = 1, MPM_K_G2P = 2, MPM_K_G2P_ADJ = 3, M
        MPM_K_COUNT = 13 };
 /* record CUDA events around every kernel launch on its stream (1 = on) */
 int mpm_profile_enable(int on);
+/* which kernel ids the profiler times while on: bit k = id k (default all).
+   Each timed launch adds two event records to its stream (graph nodes in a
+   recorded pass); a changed selection or on/off state re-records a pass. */
+int mpm_profile_select(unsigned long long mask);
 int mpm_profile_reset(void);
 /* launches and summed device time of one kernel id since the last reset */
 int mpm_profile_query(int kernel, long long* launches, double* total_ms);

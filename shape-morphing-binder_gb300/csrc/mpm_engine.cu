@@ -100,6 +100,9 @@ struct Prof {
         bool graph_owned;  // recorded by a captured graph: never returned to the pool
     };
     bool capturing = false;
+    // kernel ids timed while on (bit k: kernel id k)
+    unsigned long long mask = ~0ull;
+    bool timed(int id) const { return on && ((mask >> id) & 1ull); }
     std::vector<Rec> pending;
     std::vector<cudaEvent_t> pool;
     long long count[K_COUNT] = {0};
@@ -138,7 +141,7 @@ struct KTimer {
     cudaEvent_t a = nullptr;
     KTimer(int id_, cudaStream_t s_) : id(id_), s(s_)
     {
-        if (g_prof.on) {
+        if (g_prof.timed(id)) {
             a = g_prof.get();
             record(a);
         }
@@ -1050,6 +1053,7 @@ void run_captured(Graph& G, const std::string& key, Sig& sig, F&& body)
         return;
     }
     sig.add((unsigned long long)g_prof.on);
+    sig.add(g_prof.mask);
     auto& slot = G.caps[key];
     if (!slot) slot.reset(new Graph::Cap());
     Graph::Cap& c = *slot;
@@ -2520,6 +2524,14 @@ int mpm_profile_enable(int on)
     return guard([&] {
         g_prof.resolve();
         g_prof.on = on != 0;
+    });
+}
+
+int mpm_profile_select(unsigned long long mask)
+{
+    return guard([&] {
+        g_prof.resolve();
+        g_prof.mask = mask;
     });
 }
 

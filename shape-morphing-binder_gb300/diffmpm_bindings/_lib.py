@@ -127,6 +127,7 @@ _SIGS = {
     "mpm_compgraph_get_block_threads": [_vp, _ip],
     "mpm_compgraph_synchronize": [_vp],
     "mpm_profile_enable": [C.c_int],
+    "mpm_profile_select": [C.c_ulonglong],
     "mpm_profile_reset": [],
     "mpm_profile_query": [C.c_int, C.POINTER(C.c_longlong), _dp],
     "mpm_kernel_name": [C.c_int],
