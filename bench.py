@@ -575,7 +575,7 @@ def run_e2e(torch, dm, args, w, device, keep, tuning=None):
     cg.set_up_comp_graph(T + 1)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).pin_memory()  # noqa: E731
     hx, hv, hF = pin(w.x), pin(w.v), pin(w.F)
-    htgt = w.target.astype(np.float32)
+    htgt = torch.from_numpy(np.ascontiguousarray(w.target, dtype=np.float32))
     out_x = torch.empty((n, 3), dtype=torch.float32).pin_memory()
     out_gv = torch.empty((n, 3), dtype=torch.float32).pin_memory()
     out_gF = torch.empty((n, 3, 3), dtype=torch.float32).pin_memory()
@@ -601,7 +601,9 @@ def run_e2e(torch, dm, args, w, device, keep, tuning=None):
         cg.compute_forward_pass(0, 0)
         last = cg.get_point_cloud(T)
         get_into(last, "x", out_x)
-        np.multiply(out_x.numpy() - htgt, 2.0 / n, out=seed.numpy())
+        # host-side loss gradient, in place on the host threads (torch CPU ops)
+        torch.sub(out_x, htgt, out=seed)
+        seed.mul_(2.0 / n)
         last.set("grad_x", seed.numpy())
         cg.compute_backward_pass(0)
         get_into(l0, "grad_v", out_gv)
@@ -609,7 +611,7 @@ def run_e2e(torch, dm, args, w, device, keep, tuning=None):
         if grad_E:
             get_into(l0, "grad_lam", out_gl)
             get_into(l0, "grad_mu", out_gm)
-            return float(out_gl.numpy().sum(dtype=np.float64) * dlam + out_gm.numpy().sum(dtype=np.float64) * dmu)
+            return float(out_gl.sum(dtype=torch.float64)) * dlam + float(out_gm.sum(dtype=torch.float64)) * dmu
         return None
 
     for _ in range(max(1, min(args.warmup, 2))):
