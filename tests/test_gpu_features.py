@@ -49,7 +49,7 @@ def test_multistep_exact_matches_oracle(dm, orc, prec):
     seed_gx = rng.normal(size=(s0.n, 3)) / s0.n
     xT, g0, _, _ = _rollout(dm, s0, g, prm, T, seed_gx, prec)
     xw, gw = oracle_rollout(orc, g, prm, s0, T, seed_gx)
-    tol = 1e-9 if prec == "fp64" else 2e-4
+    tol = 1e-9 if prec == "fp64" else 1e-5  # FP32 measured <= 9.1e-7
     assert rel_err(xT, xw) < (1e-10 if prec == "fp64" else 1e-6)
     for k, want in (("x", gw.x), ("v", gw.v), ("F", gw.F), ("C", gw.C), ("dFc", gw.Ft)):
         e = norm_err(g0[k], want)

@@ -159,7 +159,7 @@ def test_compressive_rollout_matches_oracle(dm, orc, prec, adjoint):
     print(f"{prec} {adjoint}: x_T {ex:.2e}, " + ", ".join(f"g{k} {e:.2e}" for k, e in errs.items()) +
           f"; branches per step {counts}")
     assert ex < (1e-12 if prec == "fp64" else 1e-5)
-    tol = 1e-9 if prec == "fp64" else 1e-4
+    tol = 1e-9 if prec == "fp64" else 2e-5  # FP32 measured <= 1.1e-6 through every guard branch
     for k, e in errs.items():
         assert e < tol, (k, e)
 

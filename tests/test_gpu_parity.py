@@ -5,8 +5,11 @@ Tolerances: the plain FP64 engine must agree with the FP64 oracle to 1e-9
 relative (atomic summation order is the only difference).  The FP32 engine
 is held to tolerances below the reference's own FP32 noise floor on the same
 inputs (tests/golden: its float build differs from its double build by up to
-~1e-4 in C): x 1e-6, F 1e-6, v 2e-5 and C 1e-4 relative to the field's max
-magnitude, gradients 2e-3 in norm for one step.
+~1e-4 in C): x 1e-6, F 1e-6, v 5e-6 and C 1e-5 relative to the field's max
+magnitude, gradients 1e-5 in norm for one step (measured on a GB300: fields
+<= 8e-7, one-step gradients <= 6e-7, so each bound keeps a margin of 10x or
+more against the atomics' order).  The benchmark spec's bound for gradients is
+1e-4.
 """
 import numpy as np
 import pytest
@@ -17,8 +20,8 @@ from helpers import (get_grads, golden_grid, golden_params, golden_state, layer_
 
 pytestmark = pytest.mark.gpu
 
-FWD_TOL = {"fp64": dict(x=1e-9, v=1e-9, C=1e-9, F=1e-9), "fp32": dict(x=1e-6, v=2e-5, C=1e-4, F=1e-6)}
-BWD_TOL = {"fp64": 1e-9, "fp32": 2e-3}
+FWD_TOL = {"fp64": dict(x=1e-9, v=1e-9, C=1e-9, F=1e-9), "fp32": dict(x=1e-6, v=5e-6, C=1e-5, F=1e-6)}
+BWD_TOL = {"fp64": 1e-9, "fp32": 1e-5}
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
@@ -73,7 +76,7 @@ def test_mass_loss(dm, orc, golden, prec, adjoint):
     gx = cg.get_grad(0, "x", np.float64)
     e = norm_err(gx, d["gx"])
     print(f"{prec} {adjoint} loss {loss:.9g} vs {want:.9g}; dLdx norm-rel {e:.3e}")
-    assert e < (1e-4 if prec == "fp32" else 1e-9)
+    assert e < (2e-5 if prec == "fp32" else 1e-9)  # measured 1.3e-6
     for k in ("v", "F", "C"):
         assert np.abs(cg.get_grad(0, k)).max() == 0.0
 
@@ -135,4 +138,4 @@ def test_rollout_against_reference_golden(dm, golden, prec):
     for k in ("x", "v"):
         e = norm_err(got[k], golden[f"roll64_g{k}"])
         print(f"{prec} roll g{k} {e:.3e}")
-        assert e < (2e-4 if prec == "fp32" else 1e-8), k
+        assert e < (1e-5 if prec == "fp32" else 1e-8), k  # measured <= 4.1e-7
