@@ -11,7 +11,7 @@
   checkpoint every 10 steps with recomputation, density for CFL 0.45.
 
 Both run the exact adjoint.  Bars: FP64 engine 1e-9 relative; FP32 engine
-x_T within 1e-5 and gradients within 1e-4 relative (spec targets).
+x_T within 1e-5 and gradients within 1e-4 relative (the precision targets of the FP32 form).
 """
 import functools
 

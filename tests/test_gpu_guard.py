@@ -17,7 +17,7 @@ the J trust region (ForwardSimulation.cpp:135-152, kJmin = 0.6 at :13).
   engine precisions, and the FP64 engine's exact adjoint against central
   differences.
 
-FP32 bar: 1e-4 relative (spec gradient target) on P, the stress
+FP32 bar: 1e-4 relative (the gradient precision target) on P, the stress
 derivative and the rollout gradients; FP64 engine: 1e-9.
 """
 import copy

@@ -8,7 +8,7 @@ inputs (tests/golden: its float build differs from its double build by up to
 ~1e-4 in C): x 1e-6, F 1e-6, v 5e-6 and C 1e-5 relative to the field's max
 magnitude, gradients 1e-5 in norm for one step (measured on a GB300: fields
 <= 8e-7, one-step gradients <= 6e-7, so each bound keeps a margin of 10x or
-more against the atomics' order).  The benchmark spec's bound for gradients is
+more against the atomics' order).  The precision target for gradients is
 1e-4.
 """
 import numpy as np
