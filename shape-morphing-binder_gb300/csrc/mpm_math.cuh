@@ -352,13 +352,19 @@ static __host__ __device__ __noinline__ void polar_svd(const double* F, double* 
         for (int c = 0; c < 3; ++c) Rm[r * 3 + c] = u[0][r] * Vs[c * 3] + u[1][r] * Vs[c * 3 + 1] + u[2][r] * Vs[c * 3 + 2];
 }
 
-// Newton stopping rule: once the relative step is below `step` (squared
-// here), one more step is taken; convergence is quadratic, so that last step
-// lands below the precision's rounding level.  FP32: a relative step of 1e-4,
-// after which the error is ~5e-9 (a 1e-5 threshold costs one more iteration
-// for nothing FP32 can hold: P2G and its transpose 0.6% slower).
+// Newton stopping rule: the iteration stops once the relative step is below
+// `step` (squared here).  Convergence is quadratic: the step estimates the
+// previous iterate's error e, and the new iterate's error is ~e^2 / 2.  FP32:
+// a relative step of 1e-4 leaves an error of ~5e-9, below FP32 rounding, so
+// FP32 stops there (against 2.5e5 random F up to 60% stretch, the factor
+// differs from the FP64 SVD's by at most 1.7e-7 either way, the rounding of
+// F itself).  FP64 takes one more step after its 1e-8 rule.
 #ifndef MPM_POLAR_STEP2_F32
 #define MPM_POLAR_STEP2_F32 1e-8f
+#endif
+// 1: the FP32 iteration also takes the one more step (0.5-1% slower steps)
+#ifndef MPM_POLAR_EXTRA_F32
+#define MPM_POLAR_EXTRA_F32 0
 #endif
 template <typename R>
 struct Tol;
@@ -366,11 +372,13 @@ template <>
 struct Tol<float> {
     static constexpr float step2 = MPM_POLAR_STEP2_F32;
     static constexpr int iters = 10;
+    static constexpr bool extra = MPM_POLAR_EXTRA_F32 != 0;
 };
 template <>
 struct Tol<double> {
     static constexpr double step2 = 1e-16;
     static constexpr int iters = 30;
+    static constexpr bool extra = true;
 };
 
 // Scaled Newton iteration for the polar factor (Higham 1986):
@@ -405,7 +413,10 @@ MPM_HD bool polar_newton(const R* F, R* Rm)
         }
         if (diff < R(1e-4)) scale = false;
         if (last) break;
-        if (diff <= Tol<R>::step2 * ny) last = true;
+        if (diff <= Tol<R>::step2 * ny) {
+            if (!Tol<R>::extra) break;
+            last = true;
+        }
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) Rm[i] = X[i];
