@@ -2,9 +2,10 @@
 //
 // 3x3 matrices are row-major arrays of 9 scalars.  Everything is templated on
 // the storage scalar R (float for the production path, double for the plain
-// all-FP64 form).  The float path computes the polar decomposition with a
-// scaled Newton iteration in FP32 and falls back to an FP64 Jacobi SVD when
-// F is close to inversion (the FP64 guard); J - 1 is formed from F - I so the
+// all-FP64 form).  The float path computes the polar decomposition in FP32
+// (Newton-Schulz for a nearly orthogonal F, scaled Newton otherwise) and
+// falls back to an FP64 Jacobi SVD when F is close to inversion (the FP64
+// guard); J - 1 is formed from F - I so the
 // volumetric stress does not lose digits to cancellation.
 #pragma once
 #include <cuda_runtime.h>
@@ -423,6 +424,56 @@ MPM_HD bool polar_newton(const R* F, R* Rm)
     return true;
 }
 
+// Newton-Schulz iteration for the polar factor of a nearly orthogonal F:
+// X <- X (3I - X^T X) / 2.  On a singular value s = 1 + d it gives
+// 1 - 3 d^2 / 2 - d^3 / 2, quadratic like Newton's, but with no inverse or
+// reciprocal: about 40% fewer operations per iteration.  It converges for
+// every s in (0, sqrt 3); it is used only when |I - F^T F|_F^2 <= kSchulzIn
+// (every s within ~20% of 1) and returns false otherwise.  E = I - X^T X is
+// formed before each update; |d| ~ |E| / 2, so once |E|_F^2 is below
+// kSchulzOut the update leaves an error of ~3 |E|^2 / 8 < 4e-9 and is the
+// last one.
+#ifndef MPM_POLAR_SCHULZ
+#define MPM_POLAR_SCHULZ 1
+#endif
+constexpr float kSchulzIn = 0.25f, kSchulzOut = 1e-8f;
+MPM_HD bool polar_schulz(const float* F, float* Rm)
+{
+    float X[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) X[i] = F[i];
+    for (int it = 0; it < 8; ++it) {
+        // E = I - X^T X (symmetric)
+        float E[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = r; c < 3; ++c) {
+                const float m = X[r] * X[c] + X[3 + r] * X[3 + c] + X[6 + r] * X[6 + c];
+                E[r * 3 + c] = E[c * 3 + r] = (r == c ? 1.f : 0.f) - m;
+            }
+        const float e2 = E[0] * E[0] + E[4] * E[4] + E[8] * E[8] +
+                         2.f * (E[1] * E[1] + E[2] * E[2] + E[5] * E[5]);
+        if (it == 0 && !(e2 <= kSchulzIn)) return false;
+        // X <- X + X E / 2
+        float Y[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                Y[r * 3 + c] = X[r * 3 + c] + 0.5f * (X[r * 3] * E[c] + X[r * 3 + 1] * E[3 + c] + X[r * 3 + 2] * E[6 + c]);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) X[i] = Y[i];
+        if (e2 <= kSchulzOut) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Rm[i] = X[i];
+            return true;
+        }
+    }
+    return false;
+}
+MPM_HD bool polar_schulz(const double*, double*) { return false; }  // FP64 keeps Newton
+
 // Branch flags some device functions can report (a null flag pointer, the
 // default, compiles the reporting away): which guarded or clamped form ran.
 enum {
@@ -465,7 +516,7 @@ MPM_HD void polar(const R* F, R* Rm, R* S, unsigned* fl = nullptr)
     R J = det3(F);
     R n2 = dot9(F, F);
     R ref = n2 * sqrt(n2) * R(0.19245008972987526);  // (|F|_F / sqrt 3)^3
-    bool ok = (J > R(0.05) * ref) && polar_newton(F, Rm);
+    bool ok = (J > R(0.05) * ref) && ((MPM_POLAR_SCHULZ && polar_schulz(F, Rm)) || polar_newton(F, Rm));
     if (!ok) {
         // the guard works on copies, so the caller's arrays are never
         // address-taken (they stay in registers on the common path)
