@@ -1061,11 +1061,8 @@ __global__ void __launch_bounds__(kThreads, MPM_P2G_MIN_BLOCKS) k_p2g_seg(KP<flo
         load_Ft(st, dfc, ld, p, F, Ft);
         mass = co[CO_M * ld + p];
         const float vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
-        Inv<float> iv;
-        invariants(Ft, iv);
-        float P[9], Rm[9], S[9], PF[9];
-        pk(kp.material, Ft, lam, mu, iv, P, Rm, S);
-        mulNT3(P, Ft, PF);
+        float PF[9];
+        stress_pf(kp.material, Ft, lam, mu, PF);
         const float trC = C[0] + C[4] + C[8];
         const float k1 = -kp.C0 * kp.dt * vol;
 #pragma unroll
@@ -1120,11 +1117,8 @@ k_g2p2g(KP<float> kp, int n, long long ld, const float* __restrict__ st, const f
         }
         mass = co[CO_M * ld + p];
         const float vol = co[CO_VOL * ld + p], lam = co[CO_LAM * ld + p], mu = co[CO_MU * ld + p];
-        Inv<float> iv;
-        invariants(F1, iv);
-        float P[9], Rm[9], S[9], PF[9];
-        pk(kp.material, F1, lam, mu, iv, P, Rm, S);
-        mulNT3(P, F1, PF);
+        float PF[9];
+        stress_pf(kp.material, F1, lam, mu, PF);
         const float trC = C1[0] + C1[4] + C1[8];
         const float k1 = -kp.C0 * kp.dt * vol;
 #pragma unroll

@@ -599,6 +599,41 @@ MPM_HD void pk(int material, const R* F, R lam, R mu, const Inv<R>& iv, R* P, R*
     }
 }
 
+// P F^T, the stress term P2G scatters.  Where the FP32 invariants apply
+// (J > 0.25) it needs no F^{-T} (F^{-T} F^T = I): FCR 2 mu (F - R) F^T +
+// lam (J - 1) J I, Neo-Hookean mu (F F^T - I) + lam log(J) I.  Elsewhere
+// (the FP64 guard regime) it is pk's P times F^T.
+template <typename R>
+MPM_HD void stress_pf(int material, const R* F, R lam, R mu, R* PF, unsigned* fl = nullptr)
+{
+    const R jm1 = det_minus_one(F);
+    const R J = R(1) + jm1;
+    if (J > R(0.25)) {
+        R D[9], dg;
+        if (material == MAT_FCR) {
+            R Rm[9], S[9];
+            polar(F, Rm, S, fl);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) D[i] = R(2) * mu * (F[i] - Rm[i]);
+            dg = lam * jm1 * J;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) D[i] = mu * F[i];
+            dg = lam * log(J) - mu;
+        }
+        mulNT3(D, F, PF);
+        PF[0] += dg;
+        PF[4] += dg;
+        PF[8] += dg;
+        return;
+    }
+    Inv<R> iv;
+    invariants(F, iv, fl);
+    R P[9], Rm[9], S[9];
+    pk(material, F, lam, mu, iv, P, Rm, S, fl);
+    mulNT3(P, F, PF);
+}
+
 // Derivative of the polar rotation applied to G: with A = tr(S) I - S,
 // A w = axial(R^T G - G^T R) and dR = R [w]x, regularising A by 1e-4 on the
 // diagonal when det A < 1e-6 (Elasticity.cpp:57-117).
