@@ -4,10 +4,9 @@
   (gcc + OpenMP).  Built on every machine that runs the tests.
 * ``oracle/_ref/libref32.so`` / ``libref64.so`` -- the reference's own
   DiffMPMLib3D sources compiled together with ``ref_driver.cpp``.  Built only
-  where the reference tree is found: the ``REF_DIR`` environment variable
-  (the checkout's root, holding ``DiffMPMLib3D/`` and ``include/``), else the
-  build container's mount point when it exists; without it they are skipped
-  and the tests that need them skip too.  The sources
+  where the reference tree is named by the ``REF_DIR`` environment variable
+  (the checkout's root, holding ``DiffMPMLib3D/`` and ``include/``); without
+  it they are skipped and the tests that need them skip too.  The sources
   are read where they lie; the FP64 variant and the ``private:`` ->
   ``public:`` edit (so ``ref_driver.cpp`` can set CompGraph's dt, drag and
   smoothing) are applied to temporary copies outside this repository.  Only
@@ -33,18 +32,10 @@ HERE = Path(__file__).resolve().parent
 OUT_REF = HERE / "_ref"
 
 
-# where the build container mounts the reference checkout (read-only); the
-# GPU host has none, and the prebuilt oracle/_ref files travel there instead
-DEFAULT_REF = Path("/root/reference")
-
-
 def ref_dir() -> Path | None:
-    """The reference checkout named by $REF_DIR, else the default mount point
-    if it exists, else None."""
+    """The reference checkout named by $REF_DIR, or None."""
     d = os.environ.get("REF_DIR")
-    if d:
-        return Path(d)
-    return DEFAULT_REF if DEFAULT_REF.is_dir() else None
+    return Path(d) if d else None
 
 
 REF_SOURCES = [
